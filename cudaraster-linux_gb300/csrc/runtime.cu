@@ -1,0 +1,784 @@
+// runtime.cu -- host side of the C ABI (include/cudaraster.h).
+//
+// Mirrors the reference's CudaRaster host class (src/cudaraster/CudaRaster.cpp):
+// state setters with the same validation messages, the queue-capacity
+// estimate and the overflow-detect-and-rerun loop of drawTriangles
+// (CudaRaster.cpp:237-342), per-stage CUDA events for getStats
+// (CudaRaster.cpp:346-363). Errors are returned as cr_status codes with a
+// message in cr_last_error() instead of exiting the process; the C++
+// wrapper (CudaRaster.hpp) turns them into the reference's fail().
+#include "cudaraster.h"
+#include "cudaraster/detail/device.cuh"
+#include "cudaraster/detail/pipe_registry.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+namespace cr {
+cudaError_t launchBinning(const DrawDev& d, int maxBins, int numSMs, cudaStream_t stream, cudaEvent_t evCoarse);
+}
+
+using namespace cr;
+
+// ------------------------------------------------------------ pipe registry
+namespace {
+std::vector<PipeDesc>& registry() {
+    static std::vector<PipeDesc> r;
+    return r;
+}
+std::mutex& registryMutex() {
+    static std::mutex m;
+    return m;
+}
+const PipeDesc* findPipe(const char* name) {
+    std::lock_guard<std::mutex> lock(registryMutex());
+    for (const PipeDesc& p : registry())
+        if (strncmp(p.name, name, sizeof(p.name)) == 0) return &p;
+    return nullptr;
+}
+}  // namespace
+
+extern "C" void cr_register_pipe(const cr::PipeDesc* desc) {
+    std::lock_guard<std::mutex> lock(registryMutex());
+    for (PipeDesc& p : registry())
+        if (strncmp(p.name, desc->name, sizeof(p.name)) == 0) { p = *desc; return; }
+    registry().push_back(*desc);
+}
+
+// ---------------------------------------------------------- device buffers
+namespace {
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t need) {
+        if (need <= bytes) return cudaSuccess;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        size_t alloc = std::max<size_t>(need, 256);
+        cudaError_t e = cudaMalloc(&ptr, alloc);
+        if (e == cudaSuccess) bytes = alloc;
+        return e;
+    }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    template <class T> T* as() const { return (T*)ptr; }
+};
+
+struct HostInstance {
+    const PipeDesc* pipe;
+    InstanceDev dev;
+};
+}  // namespace
+
+struct cr_context {
+    std::string lastError;
+    // Surfaces (CudaRaster.cpp:132-170).
+    void* color = nullptr;
+    void* depth = nullptr;
+    int width = 0, height = 0, numSamples = 0, samplesLog2 = 0;
+    bool surfacesSet = false;
+    // Deferred clear (CudaRaster.cpp:174-179).
+    bool deferredClear = false;
+    uint32_t clearColor = 0, clearDepth = 0;
+    // Pipe and buffers.
+    const PipeDesc* pipe = nullptr;
+    const void* vertices = nullptr;
+    const void* indices = nullptr;
+    int numTris = 0;
+    bool vertexSet = false, indexSet = false;
+    cr_tuning tuning{};
+    // Capacities (elements), grown by the rerun loop and kept across draws.
+    int64_t maxSubtris = 0, maxBinEntries = 0, maxTileEntries = 0;
+    // Device memory.
+    DevBuf triSubtris, triHeader, triData, chunkBinCount, binCount, binStart, binUnitFirst, binList;
+    DevBuf unitBin, unitSeg, unitTileCount, tileCount, tileStart, tileList, instBuf, prefixBuf, counters, fineCounters;
+    // Pinned staging.
+    void* hostStage = nullptr;
+    size_t hostStageBytes = 0;
+    Counters* hostCounters = nullptr;
+    cudaEvent_t ev[5] = {};
+    bool eventsRecorded = false;
+    int numSMs = 0;
+    int device = 0;
+    // Last draw.
+    cr_counters last{};
+};
+
+namespace {
+cr_status fail(cr_context* ctx, cr_status s, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (ctx) ctx->lastError = buf;
+    return s;
+}
+cr_status cudaFail(cr_context* ctx, cudaError_t e, const char* what) {
+    return fail(ctx, e == cudaErrorMemoryAllocation ? CR_ERR_OUT_OF_MEMORY : CR_ERR_CUDA, "CudaRaster: %s failed: %s",
+                what, cudaGetErrorString(e));
+}
+#define CR_CUDA(call, what)                              \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return cudaFail(ctx, e_, what); \
+    } while (0)
+
+int ilog2(int v) {
+    int r = 0;
+    while ((1 << r) < v) r++;
+    return r;
+}
+
+// Host arithmetic of the reference.
+uint32_t hostChannel(float c) {  // Math.cpp:41-48
+    float cl = std::fmin(std::fmax(c, 0.0f), 1.0f);
+    uint64_t t = (uint64_t)((double)cl * std::exp2(56.0));
+    return (uint32_t)((((t * 255) >> 55) + 1) >> 1);
+}
+uint32_t encodeDepth(uint32_t depth) {  // Util.hpp:290-298
+    double v = (double)depth;
+    v /= 65536.0 * 65536.0 - 1.0;
+    v = std::min(std::max(v, 0.0), 1.0);
+    v *= (double)(kDepthMax - kDepthMin);
+    v += (double)kDepthMin;
+    return (uint32_t)v;
+}
+}  // namespace
+
+// ================================================================ C API
+extern "C" {
+
+int32_t cr_abi_version(void) { return CR_ABI_VERSION; }
+
+const char* cr_status_string(cr_status s) {
+    switch (s) {
+    case CR_OK: return "CR_OK";
+    case CR_ERR_INVALID_ARGUMENT: return "CR_ERR_INVALID_ARGUMENT";
+    case CR_ERR_INVALID_STATE: return "CR_ERR_INVALID_STATE";
+    case CR_ERR_NO_PIPE: return "CR_ERR_NO_PIPE";
+    case CR_ERR_PIPE_MISMATCH: return "CR_ERR_PIPE_MISMATCH";
+    case CR_ERR_CAPACITY: return "CR_ERR_CAPACITY";
+    case CR_ERR_CUDA: return "CR_ERR_CUDA";
+    case CR_ERR_TIMEOUT: return "CR_ERR_TIMEOUT";
+    case CR_ERR_OUT_OF_MEMORY: return "CR_ERR_OUT_OF_MEMORY";
+    case CR_ERR_UNSUPPORTED: return "CR_ERR_UNSUPPORTED";
+    }
+    return "CR_ERR_UNKNOWN";
+}
+
+const char* cr_last_error(const cr_context* ctx) { return ctx ? ctx->lastError.c_str() : ""; }
+
+uint32_t cr_color_to_abgr(float r, float g, float b, float a) {
+    return hostChannel(r) | (hostChannel(g) << 8) | (hostChannel(b) << 16) | (hostChannel(a) << 24);
+}
+uint32_t cr_encode_depth(uint32_t d) { return encodeDepth(d); }
+uint32_t cr_decode_depth(uint32_t depth) {  // Util.hpp:302-310
+    double v = (double)depth;
+    v -= (double)kDepthMin;
+    v *= 1.0 / (double)(kDepthMax - kDepthMin);
+    v = std::min(std::max(v, 0.0), 1.0);
+    v *= 65536.0 * 65536.0 - 1.0;
+    return (uint32_t)v;
+}
+uint32_t cr_clear_depth_from_float(float depth) {  // CudaRaster.cpp:178
+    double v = (double)depth * std::exp2(32.0);
+    uint64_t t;
+    if (!(v > 0.0)) t = 0;
+    else if (v >= 18446744073709551616.0) t = UINT64_MAX;
+    else t = (uint64_t)v;
+    return encodeDepth((uint32_t)std::min<uint64_t>(t, 0xFFFFFFFFull));
+}
+
+cr_status cr_create(cr_context** out) {
+    if (!out) return CR_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) return CR_ERR_CUDA;  // "No CUDA-capable devices found!"
+    cr_context* ctx = new cr_context();
+    cudaGetDevice(&ctx->device);
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, ctx->device) != cudaSuccess) { delete ctx; return CR_ERR_CUDA; }
+    if (prop.major < 10) {  // the kernels are built for sm_103a only
+        delete ctx;
+        return CR_ERR_UNSUPPORTED;
+    }
+    ctx->numSMs = prop.multiProcessorCount;
+    for (int i = 0; i < 5; i++) {
+        if (cudaEventCreate(&ctx->ev[i]) != cudaSuccess) { delete ctx; return CR_ERR_CUDA; }
+    }
+    if (cudaMallocHost(&ctx->hostCounters, sizeof(Counters)) != cudaSuccess) { delete ctx; return CR_ERR_CUDA; }
+    memset(ctx->hostCounters, 0, sizeof(Counters));
+    *out = ctx;
+    return CR_OK;
+}
+
+cr_status cr_destroy(cr_context* ctx) {
+    if (!ctx) return CR_ERR_INVALID_ARGUMENT;
+    cudaDeviceSynchronize();
+    DevBuf* bufs[] = {&ctx->triSubtris, &ctx->triHeader, &ctx->triData, &ctx->chunkBinCount, &ctx->binCount,
+                      &ctx->binStart, &ctx->binUnitFirst, &ctx->binList, &ctx->unitBin, &ctx->unitSeg,
+                      &ctx->unitTileCount, &ctx->tileCount, &ctx->tileStart, &ctx->tileList, &ctx->instBuf,
+                      &ctx->prefixBuf, &ctx->counters, &ctx->fineCounters};
+    for (DevBuf* b : bufs) b->release();
+    if (ctx->hostStage) cudaFreeHost(ctx->hostStage);
+    if (ctx->hostCounters) cudaFreeHost(ctx->hostCounters);
+    for (int i = 0; i < 5; i++)
+        if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+    delete ctx;
+    return CR_OK;
+}
+
+cr_status cr_set_surfaces(cr_context* ctx, void* color, void* depth, int32_t width, int32_t height, int32_t num_samples) {
+    if (!ctx) return CR_ERR_INVALID_ARGUMENT;
+    if (!color && !depth) {
+        ctx->surfacesSet = false;
+        ctx->color = ctx->depth = nullptr;
+        return CR_OK;
+    }
+    if (!color) return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaRaster: No color buffer specified!");
+    if (!depth) return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaRaster: No depth buffer specified!");
+    if (width <= 0 || height <= 0) return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaSurface: Size must be positive!");
+    if (width > CR_MAX_VIEWPORT || height > CR_MAX_VIEWPORT)
+        return fail(ctx, CR_ERR_CAPACITY, "CudaSurface: CR_MAXVIEWPORT_SIZE exceeded!");
+    if (num_samples > 8) return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaSurface: numSamples cannot exceed 8!");
+    if (num_samples < 1 || (num_samples & (num_samples - 1)))
+        return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaSurface: numSamples must be a power of two!");
+    if (((uintptr_t)color & 3) || ((uintptr_t)depth & 3))
+        return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaRaster: surfaces must be 4-byte aligned!");
+    ctx->color = color;
+    ctx->depth = depth;
+    ctx->width = width;
+    ctx->height = height;
+    ctx->numSamples = num_samples;
+    ctx->samplesLog2 = ilog2(num_samples);
+    ctx->surfacesSet = true;
+    return CR_OK;
+}
+
+cr_status cr_deferred_clear(cr_context* ctx, float r, float g, float b, float a, float depth) {
+    if (!ctx) return CR_ERR_INVALID_ARGUMENT;
+    ctx->deferredClear = true;
+    ctx->clearColor = cr_color_to_abgr(r, g, b, a);
+    ctx->clearDepth = cr_clear_depth_from_float(depth);
+    return CR_OK;
+}
+
+cr_status cr_deferred_clear_raw(cr_context* ctx, uint32_t abgr, uint32_t encoded_depth) {
+    if (!ctx) return CR_ERR_INVALID_ARGUMENT;
+    ctx->deferredClear = true;
+    ctx->clearColor = abgr;
+    ctx->clearDepth = encoded_depth;
+    return CR_OK;
+}
+
+cr_status cr_set_pixel_pipe(cr_context* ctx, const char* name) {
+    if (!ctx) return CR_ERR_INVALID_ARGUMENT;
+    if (!name) {
+        ctx->pipe = nullptr;
+        return CR_OK;
+    }
+    const PipeDesc* p = findPipe(name);
+    if (!p) return fail(ctx, CR_ERR_NO_PIPE, "CudaRaster: Invalid pixel pipe!");
+    ctx->pipe = p;
+    return CR_OK;
+}
+
+cr_status cr_set_vertex_buffer(cr_context* ctx, const void* vertices, int64_t offset_bytes) {
+    if (!ctx) return CR_ERR_INVALID_ARGUMENT;
+    if (!vertices) {
+        ctx->vertexSet = false;
+        ctx->vertices = nullptr;
+        return CR_OK;
+    }
+    const char* p = (const char*)vertices + offset_bytes;
+    if ((uintptr_t)p & 15) return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaRaster: vertex buffer must be 16-byte aligned!");
+    ctx->vertices = p;
+    ctx->vertexSet = true;
+    return CR_OK;
+}
+
+cr_status cr_set_index_buffer(cr_context* ctx, const void* indices, int64_t offset_bytes, int32_t num_tris) {
+    if (!ctx) return CR_ERR_INVALID_ARGUMENT;
+    if (!indices) {
+        ctx->indexSet = false;
+        ctx->indices = nullptr;
+        return CR_OK;
+    }
+    if (num_tris < 0 || num_tris > CR_MAX_TRIANGLES)
+        return fail(ctx, CR_ERR_CAPACITY, "CudaRaster: CR_MAXSUBTRIS_SIZE exceeded!");
+    const char* p = (const char*)indices + offset_bytes;
+    if ((uintptr_t)p & 3) return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaRaster: index buffer must be 4-byte aligned!");
+    ctx->indices = p;
+    ctx->numTris = num_tris;
+    ctx->indexSet = true;
+    return CR_OK;
+}
+
+cr_status cr_set_tuning(cr_context* ctx, const cr_tuning* t) {
+    if (!ctx) return CR_ERR_INVALID_ARGUMENT;
+    if (!t) {
+        ctx->tuning = cr_tuning{};
+        return CR_OK;
+    }
+    if (t->bin_log2 > 0 && (t->bin_log2 < 3 || t->bin_log2 > 5))
+        return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaRaster: bin_log2 must be 3, 4 or 5");
+    if (t->fine_warps > 0 && (t->fine_warps > 8 || (t->fine_warps & (t->fine_warps - 1))))
+        return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaRaster: fine_warps must be 1, 2, 4 or 8");
+    if (t->bin_chunk_tris > 0 && (t->bin_chunk_tris % 512))
+        return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaRaster: bin_chunk_tris must be a multiple of 512");
+    ctx->tuning = *t;
+    return CR_OK;
+}
+
+cr_status cr_set_debug_params(cr_context* ctx, const cr_debug_params* p) {
+    if (!ctx) return CR_ERR_INVALID_ARGUMENT;
+    if (p && (p->emulate_triangle_setup || p->emulate_bin_raster || p->emulate_coarse_raster || p->emulate_fine_raster))
+        return fail(ctx, CR_ERR_UNSUPPORTED, "CudaRaster: host emulation of pipeline stages is not provided");
+    return CR_OK;
+}
+
+cr_status cr_set_capacity(cr_context* ctx, int64_t ms, int64_t mb, int64_t mt) {
+    if (!ctx) return CR_ERR_INVALID_ARGUMENT;
+    if (ms < 0 || mb < 0 || mt < 0) return CR_ERR_INVALID_ARGUMENT;
+    ctx->maxSubtris = ms;
+    ctx->maxBinEntries = mb;
+    ctx->maxTileEntries = mt;
+    return CR_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ drawing
+namespace {
+
+struct Plan {
+    std::vector<HostInstance> inst;
+    std::vector<int32_t> chunkPrefix, binPrefix, tilePrefix;
+    std::vector<int64_t> triPrefix;
+    struct Group { const PipeDesc* pipe; int instBegin, instEnd; int64_t triBegin, triEnd; int32_t tileBegin, tileEnd; };
+    std::vector<Group> groups;
+    int64_t totalTris = 0, chunkCountEntries = 0;
+    int32_t totalBins = 0, totalTiles = 0, totalChunks = 0, maxBins = 0;
+    int binLog2 = 4, unitEntries = 2048;
+};
+
+cr_status buildPlan(cr_context* ctx, const std::vector<HostInstance>& in, Plan& plan) {
+    plan.binLog2 = ctx->tuning.bin_log2 > 0 ? ctx->tuning.bin_log2 : 4;
+    plan.unitEntries = ctx->tuning.coarse_unit_entries > 0 ? ctx->tuning.coarse_unit_entries : 2048;
+    // Group instances by pipe, keeping first-seen pipe order (outputs do not depend on it).
+    std::vector<const PipeDesc*> order;
+    for (const HostInstance& h : in)
+        if (std::find(order.begin(), order.end(), h.pipe) == order.end()) order.push_back(h.pipe);
+    for (const PipeDesc* p : order)
+        for (const HostInstance& h : in)
+            if (h.pipe == p) plan.inst.push_back(h);
+    const int side = 1 << plan.binLog2;
+    int64_t tri = 0;
+    int32_t bins = 0, tiles = 0, chunks = 0;
+    int64_t countBase = 0;
+    for (size_t i = 0; i < plan.inst.size(); i++) {
+        InstanceDev& d = plan.inst[i].dev;
+        d.widthTiles = (d.width + 7) >> 3;
+        d.heightTiles = (d.height + 7) >> 3;
+        d.widthBins = (d.widthTiles + side - 1) / side;
+        d.heightBins = (d.heightTiles + side - 1) / side;
+        int nb = d.widthBins * d.heightBins;
+        if (nb > 1024)
+            return fail(ctx, CR_ERR_CAPACITY, "CudaRaster: %d bins exceed 1024; use a larger bin_log2", nb);
+        plan.maxBins = std::max(plan.maxBins, nb);
+        d.rowWords = (int64_t)(d.widthTiles * 8) << d.samplesLog2;
+        d.triBase = tri;
+        d.binBase = bins;
+        d.tileBase = tiles;
+        int chunkTris = ctx->tuning.bin_chunk_tris;
+        if (chunkTris <= 0) {
+            int64_t want = (int64_t)d.numTris / std::max(1, ctx->numSMs * 4);
+            want = (want + 511) / 512 * 512;
+            chunkTris = (int)std::min<int64_t>(std::max<int64_t>(want, 2048), 65536);
+        }
+        d.chunkTris = chunkTris;
+        d.numChunks = (d.numTris + chunkTris - 1) / chunkTris;
+        d.chunkBase = chunks;
+        d.chunkCountBase = countBase;
+        countBase += (int64_t)d.numChunks * nb;
+        tri += d.numTris;
+        bins += nb;
+        tiles += d.widthTiles * d.heightTiles;
+        chunks += d.numChunks;
+        if (tri > CR_MAX_TRIANGLES) return fail(ctx, CR_ERR_CAPACITY, "CudaRaster: CR_MAXSUBTRIS_SIZE exceeded!");
+    }
+    plan.totalTris = tri;
+    plan.totalBins = bins;
+    plan.totalTiles = tiles;
+    plan.totalChunks = chunks;
+    plan.chunkCountEntries = countBase;
+    for (const HostInstance& h : plan.inst) {
+        plan.chunkPrefix.push_back(h.dev.chunkBase);
+        plan.binPrefix.push_back(h.dev.binBase);
+        plan.tilePrefix.push_back(h.dev.tileBase);
+        plan.triPrefix.push_back(h.dev.triBase);
+    }
+    plan.chunkPrefix.push_back(chunks);
+    plan.binPrefix.push_back(bins);
+    plan.tilePrefix.push_back(tiles);
+    plan.triPrefix.push_back(tri);
+    for (size_t i = 0; i < plan.inst.size();) {
+        size_t j = i;
+        while (j < plan.inst.size() && plan.inst[j].pipe == plan.inst[i].pipe) j++;
+        Plan::Group g;
+        g.pipe = plan.inst[i].pipe;
+        g.instBegin = (int)i;
+        g.instEnd = (int)j;
+        g.triBegin = plan.inst[i].dev.triBase;
+        g.triEnd = (j < plan.inst.size()) ? plan.inst[j].dev.triBase : tri;
+        g.tileBegin = plan.inst[i].dev.tileBase;
+        g.tileEnd = (j < plan.inst.size()) ? plan.inst[j].dev.tileBase : tiles;
+        for (size_t k = i; k < j; k++) plan.inst[k].dev.pipeGroup = (int)plan.groups.size();
+        plan.groups.push_back(g);
+        i = j;
+    }
+    return CR_OK;
+}
+
+cr_status ensureCapacity(cr_context* ctx, const Plan& plan) {
+    int64_t T = plan.totalTris;
+    // Initial sizes in the spirit of CudaRaster.cpp:263-275 (subtriangle
+    // slack 4096; queues scaled with the triangle count), grown on overflow.
+    ctx->maxSubtris = std::max<int64_t>(ctx->maxSubtris, T + 4096);
+    ctx->maxBinEntries = std::max<int64_t>(ctx->maxBinEntries, 2 * T + 65536);
+    ctx->maxTileEntries = std::max<int64_t>(ctx->maxTileEntries, 4 * T + 65536);
+    const int tpb = 1 << (2 * plan.binLog2);
+    int64_t maxUnits = ctx->maxBinEntries / plan.unitEntries + plan.totalBins + 1;
+    CR_CUDA(ctx->triSubtris.ensure((size_t)std::max<int64_t>(T, 1)), "cudaMalloc");
+    CR_CUDA(ctx->triHeader.ensure((size_t)ctx->maxSubtris * 16), "cudaMalloc");
+    CR_CUDA(ctx->triData.ensure((size_t)ctx->maxSubtris * 64), "cudaMalloc");
+    CR_CUDA(ctx->chunkBinCount.ensure((size_t)std::max<int64_t>(plan.chunkCountEntries, 1) * 4), "cudaMalloc");
+    CR_CUDA(ctx->binCount.ensure((size_t)plan.totalBins * 4), "cudaMalloc");
+    CR_CUDA(ctx->binStart.ensure((size_t)plan.totalBins * 4), "cudaMalloc");
+    CR_CUDA(ctx->binUnitFirst.ensure((size_t)plan.totalBins * 4), "cudaMalloc");
+    CR_CUDA(ctx->binList.ensure((size_t)ctx->maxBinEntries * 4), "cudaMalloc");
+    CR_CUDA(ctx->unitBin.ensure((size_t)maxUnits * 4), "cudaMalloc");
+    CR_CUDA(ctx->unitSeg.ensure((size_t)maxUnits * 4), "cudaMalloc");
+    CR_CUDA(ctx->unitTileCount.ensure((size_t)maxUnits * tpb * 4), "cudaMalloc");
+    CR_CUDA(ctx->tileCount.ensure((size_t)plan.totalTiles * 4), "cudaMalloc");
+    CR_CUDA(ctx->tileStart.ensure((size_t)plan.totalTiles * 4), "cudaMalloc");
+    CR_CUDA(ctx->tileList.ensure((size_t)ctx->maxTileEntries * 4), "cudaMalloc");
+    CR_CUDA(ctx->counters.ensure(sizeof(Counters)), "cudaMalloc");
+    CR_CUDA(ctx->fineCounters.ensure(sizeof(int32_t) * std::max<size_t>(plan.groups.size(), 1)), "cudaMalloc");
+    size_t instBytes = sizeof(InstanceDev) * plan.inst.size();
+    size_t prefBytes = 4 * 3 * (plan.inst.size() + 1) + 8 * (plan.inst.size() + 1) + 64;
+    CR_CUDA(ctx->instBuf.ensure(instBytes), "cudaMalloc");
+    CR_CUDA(ctx->prefixBuf.ensure(prefBytes), "cudaMalloc");
+    size_t stage = instBytes + prefBytes;
+    if (stage > ctx->hostStageBytes) {
+        if (ctx->hostStage) cudaFreeHost(ctx->hostStage);
+        ctx->hostStage = nullptr;
+        ctx->hostStageBytes = 0;
+        CR_CUDA(cudaMallocHost(&ctx->hostStage, stage * 2), "cudaMallocHost");
+        ctx->hostStageBytes = stage * 2;
+    }
+    return CR_OK;
+}
+
+DrawDev makeDrawDev(cr_context* ctx, const Plan& plan) {
+    DrawDev d{};
+    d.inst = ctx->instBuf.as<InstanceDev>();
+    d.numInstances = (int)plan.inst.size();
+    d.binLog2 = plan.binLog2;
+    d.totalBins = plan.totalBins;
+    d.totalTiles = plan.totalTiles;
+    d.totalChunks = plan.totalChunks;
+    d.unitEntries = plan.unitEntries;
+    d.totalTris = plan.totalTris;
+    d.triSubtris = ctx->triSubtris.as<uint8_t>();
+    d.triHeader = ctx->triHeader.as<uint4>();
+    d.triData = ctx->triData.as<uint4>();
+    d.maxSubtris = ctx->maxSubtris;
+    d.chunkBinCount = ctx->chunkBinCount.as<int32_t>();
+    d.binCount = ctx->binCount.as<int32_t>();
+    d.binStart = ctx->binStart.as<int32_t>();
+    d.binUnitFirst = ctx->binUnitFirst.as<int32_t>();
+    d.binList = ctx->binList.as<uint32_t>();
+    d.maxBinEntries = ctx->maxBinEntries;
+    d.unitBin = ctx->unitBin.as<int32_t>();
+    d.unitSeg = ctx->unitSeg.as<int32_t>();
+    d.unitTileCount = ctx->unitTileCount.as<int32_t>();
+    d.maxUnits = ctx->maxBinEntries / plan.unitEntries + plan.totalBins + 1;
+    d.tileCount = ctx->tileCount.as<int32_t>();
+    d.tileStart = ctx->tileStart.as<int32_t>();
+    d.tileList = ctx->tileList.as<uint32_t>();
+    d.maxTileEntries = ctx->maxTileEntries;
+    char* pref = ctx->prefixBuf.as<char>();
+    size_t n1 = plan.inst.size() + 1;
+    d.triPrefix = (const int64_t*)pref;
+    d.chunkPrefix = (const int32_t*)(pref + 8 * n1);
+    d.binPrefix = d.chunkPrefix + n1;
+    d.tilePrefix = d.binPrefix + n1;
+    d.counters = ctx->counters.as<Counters>();
+    d.fineTileCounter = ctx->fineCounters.as<int32_t>();
+    return d;
+}
+
+cr_status launchDraw(cr_context* ctx, const Plan& plan, cudaStream_t stream) {
+    DrawDev d = makeDrawDev(ctx, plan);
+    // Stage the descriptors through pinned memory.
+    size_t n1 = plan.inst.size() + 1;
+    size_t instBytes = sizeof(InstanceDev) * plan.inst.size();
+    char* hs = (char*)ctx->hostStage;
+    for (size_t i = 0; i < plan.inst.size(); i++) memcpy(hs + i * sizeof(InstanceDev), &plan.inst[i].dev, sizeof(InstanceDev));
+    char* hp = hs + instBytes;
+    memcpy(hp, plan.triPrefix.data(), 8 * n1);
+    memcpy(hp + 8 * n1, plan.chunkPrefix.data(), 4 * n1);
+    memcpy(hp + 12 * n1, plan.binPrefix.data(), 4 * n1);
+    memcpy(hp + 16 * n1, plan.tilePrefix.data(), 4 * n1);
+    CR_CUDA(cudaMemcpyAsync(ctx->instBuf.ptr, hs, instBytes, cudaMemcpyHostToDevice, stream), "cudaMemcpyAsync");
+    CR_CUDA(cudaMemcpyAsync(ctx->prefixBuf.ptr, hp, 20 * n1, cudaMemcpyHostToDevice, stream), "cudaMemcpyAsync");
+    CR_CUDA(cudaMemsetAsync(ctx->counters.ptr, 0, sizeof(Counters), stream), "cudaMemsetAsync");
+    CR_CUDA(cudaMemsetAsync(ctx->fineCounters.ptr, 0, sizeof(int32_t) * plan.groups.size(), stream), "cudaMemsetAsync");
+
+    CR_CUDA(cudaEventRecord(ctx->ev[0], stream), "cudaEventRecord");
+    for (const Plan::Group& g : plan.groups)
+        CR_CUDA(g.pipe->launchSetup(d, g.instBegin, g.instEnd, g.triBegin, g.triEnd, stream), "setup launch");
+    CR_CUDA(cudaEventRecord(ctx->ev[1], stream), "cudaEventRecord");
+    CR_CUDA(launchBinning(d, plan.maxBins, ctx->numSMs, stream, ctx->ev[2]), "bin/coarse launch");
+    CR_CUDA(cudaEventRecord(ctx->ev[3], stream), "cudaEventRecord");
+    int warps = ctx->tuning.fine_warps > 0 ? ctx->tuning.fine_warps : 8;
+    for (size_t gi = 0; gi < plan.groups.size(); gi++) {
+        const Plan::Group& g = plan.groups[gi];
+        int ctas = ctx->tuning.fine_ctas_per_sm > 0 ? ctx->tuning.fine_ctas_per_sm : g.pipe->fineOccupancy(warps);
+        CR_CUDA(g.pipe->launchFine(d, (int)gi, g.tileBegin, g.tileEnd, warps, ctas, ctx->numSMs, stream), "fine launch");
+    }
+    CR_CUDA(cudaEventRecord(ctx->ev[4], stream), "cudaEventRecord");
+    ctx->eventsRecorded = true;
+    CR_CUDA(cudaMemcpyAsync(ctx->hostCounters, ctx->counters.ptr, sizeof(Counters), cudaMemcpyDeviceToHost, stream),
+            "cudaMemcpyAsync");
+    return CR_OK;
+}
+
+void recordCounters(cr_context* ctx, const Plan& plan, int reruns) {
+    const Counters& c = *ctx->hostCounters;
+    ctx->last.num_tris = plan.totalTris;
+    ctx->last.num_subtris = plan.totalTris + c.extraSubtris;
+    ctx->last.bin_entries = c.binEntries;
+    ctx->last.tile_entries = c.tileEntries;
+    ctx->last.coarse_units = c.numUnits;
+    ctx->last.max_subtris = ctx->maxSubtris;
+    ctx->last.max_bin_entries = ctx->maxBinEntries;
+    ctx->last.max_tile_entries = ctx->maxTileEntries;
+    ctx->last.reruns = reruns;
+    ctx->last.overflow = c.overflow;
+    ctx->last.num_bins = plan.totalBins;
+    ctx->last.num_tiles = plan.totalTiles;
+}
+
+// Overflow-detect-and-rerun (CudaRaster.cpp:277-339).
+cr_status drawPlan(cr_context* ctx, const Plan& plan, cudaStream_t stream, bool sync) {
+    cr_status st = ensureCapacity(ctx, plan);
+    if (st != CR_OK) return st;
+    for (int reruns = 0;; reruns++) {
+        st = launchDraw(ctx, plan, stream);
+        if (st != CR_OK) return st;
+        if (!sync) {
+            ctx->last.reruns = 0;
+            return CR_OK;
+        }
+        CR_CUDA(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+        recordCounters(ctx, plan, reruns);
+        const Counters& c = *ctx->hostCounters;
+        if (!c.overflow) return CR_OK;
+        if (reruns >= 16) return fail(ctx, CR_ERR_CAPACITY, "CudaRaster: queues keep overflowing");
+        int64_t subtris = plan.totalTris + c.extraSubtris;
+        if (c.overflow & kOverflowSubtris) ctx->maxSubtris = std::max(ctx->maxSubtris, subtris + 4096);
+        if (c.overflow & kOverflowBin) ctx->maxBinEntries = std::max<int64_t>(ctx->maxBinEntries, (int64_t)c.binEntries + 65536);
+        if (c.overflow & kOverflowTile) ctx->maxTileEntries = std::max<int64_t>(ctx->maxTileEntries, (int64_t)c.tileEntries + 65536);
+        if (ctx->maxSubtris > (int64_t)CR_MAX_TRIANGLES)
+            return fail(ctx, CR_ERR_CAPACITY, "CudaRaster: CR_MAXSUBTRIS_SIZE exceeded!");
+        st = ensureCapacity(ctx, plan);
+        if (st != CR_OK) return st;
+    }
+}
+
+cr_status drawCurrent(cr_context* ctx, void* stream, bool sync) {
+    if (!ctx) return CR_ERR_INVALID_ARGUMENT;
+    if (!ctx->surfacesSet) return fail(ctx, CR_ERR_INVALID_STATE, "CudaRaster: Surfaces not set!");
+    if (!ctx->pipe) return fail(ctx, CR_ERR_INVALID_STATE, "CudaRaster: Pixel pipe not set!");
+    if (!ctx->vertexSet) return fail(ctx, CR_ERR_INVALID_STATE, "CudaRaster: Vertex buffer not set!");
+    if (!ctx->indexSet) return fail(ctx, CR_ERR_INVALID_STATE, "CudaRaster: Index buffer not set!");
+    if (ctx->pipe->samplesLog2 != ctx->samplesLog2)
+        return fail(ctx, CR_ERR_PIPE_MISMATCH, "CudaRaster: Mismatch in multisampling between pixel pipe and surface!");
+    HostInstance h;
+    memset(&h.dev, 0, sizeof(h.dev));
+    h.pipe = ctx->pipe;
+    h.dev.vertices = (const float4*)ctx->vertices;
+    h.dev.indices = (const int*)ctx->indices;
+    h.dev.color = (uint32_t*)ctx->color;
+    h.dev.depth = (uint32_t*)ctx->depth;
+    h.dev.stride4 = ctx->pipe->vertexStructSize / 16;
+    h.dev.numTris = ctx->numTris;
+    h.dev.width = ctx->width;
+    h.dev.height = ctx->height;
+    h.dev.samplesLog2 = ctx->samplesLog2;
+    h.dev.deferredClear = ctx->deferredClear ? 1 : 0;
+    h.dev.clearColor = ctx->clearColor;
+    h.dev.clearDepth = ctx->clearDepth;
+    Plan plan;
+    std::vector<HostInstance> v{h};
+    cr_status st = buildPlan(ctx, v, plan);
+    if (st != CR_OK) return st;
+    st = drawPlan(ctx, plan, (cudaStream_t)stream, sync);
+    if (st == CR_OK) ctx->deferredClear = false;  // CudaRaster.cpp:341
+    return st;
+}
+
+cr_status drawBatch(cr_context* ctx, const cr_instance* instances, int32_t count, void* stream, bool sync) {
+    if (!ctx || (!instances && count > 0) || count < 0) return CR_ERR_INVALID_ARGUMENT;
+    std::vector<HostInstance> v;
+    for (int i = 0; i < count; i++) {
+        const cr_instance& s = instances[i];
+        const PipeDesc* p = s.pipe ? findPipe(s.pipe) : nullptr;
+        if (!p) return fail(ctx, CR_ERR_NO_PIPE, "CudaRaster: Invalid pixel pipe! (instance %d)", i);
+        if (!s.color || !s.depth) return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaRaster: instance %d has no surfaces", i);
+        if (s.width <= 0 || s.height <= 0 || s.width > CR_MAX_VIEWPORT || s.height > CR_MAX_VIEWPORT)
+            return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaSurface: bad size in instance %d", i);
+        int ns = s.num_samples;
+        if (ns < 1 || ns > 8 || (ns & (ns - 1))) return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaSurface: bad sample count in instance %d", i);
+        if (p->samplesLog2 != ilog2(ns))
+            return fail(ctx, CR_ERR_PIPE_MISMATCH, "CudaRaster: Mismatch in multisampling between pixel pipe and surface! (instance %d)", i);
+        if (s.num_tris < 0 || (s.num_tris > 0 && (!s.vertices || !s.indices)))
+            return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaRaster: instance %d has no geometry", i);
+        if (((uintptr_t)s.vertices & 15) || ((uintptr_t)s.indices & 3))
+            return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaRaster: misaligned buffers in instance %d", i);
+        HostInstance h;
+        memset(&h.dev, 0, sizeof(h.dev));
+        h.pipe = p;
+        h.dev.vertices = (const float4*)s.vertices;
+        h.dev.indices = (const int*)s.indices;
+        h.dev.color = (uint32_t*)s.color;
+        h.dev.depth = (uint32_t*)s.depth;
+        h.dev.stride4 = p->vertexStructSize / 16;
+        h.dev.numTris = s.num_tris;
+        h.dev.width = s.width;
+        h.dev.height = s.height;
+        h.dev.samplesLog2 = ilog2(ns);
+        h.dev.deferredClear = s.deferred_clear ? 1 : 0;
+        h.dev.clearColor = s.clear_color;
+        h.dev.clearDepth = s.clear_depth;
+        v.push_back(h);
+    }
+    if (v.empty()) return CR_OK;
+    Plan plan;
+    cr_status st = buildPlan(ctx, v, plan);
+    if (st != CR_OK) return st;
+    return drawPlan(ctx, plan, (cudaStream_t)stream, sync);
+}
+
+}  // namespace
+
+extern "C" {
+
+cr_status cr_draw_triangles(cr_context* ctx, void* stream) { return drawCurrent(ctx, stream, true); }
+cr_status cr_draw_triangles_async(cr_context* ctx, void* stream) { return drawCurrent(ctx, stream, false); }
+cr_status cr_draw_batch(cr_context* ctx, const cr_instance* inst, int32_t n, void* stream) {
+    return drawBatch(ctx, inst, n, stream, true);
+}
+cr_status cr_draw_batch_async(cr_context* ctx, const cr_instance* inst, int32_t n, void* stream) {
+    return drawBatch(ctx, inst, n, stream, false);
+}
+
+cr_status cr_get_stats(cr_context* ctx, cr_stats* out) {
+    if (!ctx || !out) return CR_ERR_INVALID_ARGUMENT;
+    memset(out, 0, sizeof(*out));
+    if (!ctx->eventsRecorded) return CR_OK;
+    CR_CUDA(cudaEventSynchronize(ctx->ev[4]), "cudaEventSynchronize");
+    float t[4] = {0, 0, 0, 0};
+    for (int i = 0; i < 4; i++) cudaEventElapsedTime(&t[i], ctx->ev[i], ctx->ev[i + 1]);
+    out->setup_time = t[0] * 1e-3f;
+    out->bin_time = t[1] * 1e-3f;
+    out->coarse_time = t[2] * 1e-3f;
+    out->fine_time = t[3] * 1e-3f;
+    return CR_OK;
+}
+
+cr_status cr_get_counters(cr_context* ctx, cr_counters* out) {
+    if (!ctx || !out) return CR_ERR_INVALID_ARGUMENT;
+    if (ctx->eventsRecorded) {
+        CR_CUDA(cudaEventSynchronize(ctx->ev[4]), "cudaEventSynchronize");
+        // The counters copy follows the last event on the same stream.
+        cudaDeviceSynchronize();
+        const Counters& c = *ctx->hostCounters;
+        ctx->last.num_subtris = ctx->last.num_tris + c.extraSubtris;
+        ctx->last.bin_entries = c.binEntries;
+        ctx->last.tile_entries = c.tileEntries;
+        ctx->last.coarse_units = c.numUnits;
+        ctx->last.overflow = c.overflow;
+    }
+    *out = ctx->last;
+    return CR_OK;
+}
+
+cr_status cr_get_profiling_info(cr_context* ctx, char* buffer, int64_t size) {
+    if (!ctx || !buffer || size <= 0) return CR_ERR_INVALID_ARGUMENT;
+    cr_stats s;
+    cr_status st = cr_get_stats(ctx, &s);
+    if (st != CR_OK) return st;
+    cr_counters c;
+    cr_get_counters(ctx, &c);
+    // Format follows getProfilingInfo's default mode (CudaRaster.cpp:367-421):
+    // stage times, then the memory footprint of the intermediate queues.
+    double mb = 1.0 / (1024.0 * 1024.0);
+    snprintf(buffer, (size_t)size,
+             "Setup  %8.3f ms\nBin    %8.3f ms\nCoarse %8.3f ms\nFine   %8.3f ms\nTotal  %8.3f ms\n"
+             "Triangles     %lld\nSubtriangles  %lld (%.1f MB)\nBin entries   %lld (%.1f MB)\n"
+             "Tile entries  %lld (%.1f MB)\nCoarse units  %lld\nReruns        %d\n",
+             s.setup_time * 1e3, s.bin_time * 1e3, s.coarse_time * 1e3, s.fine_time * 1e3,
+             (s.setup_time + s.bin_time + s.coarse_time + s.fine_time) * 1e3, (long long)c.num_tris,
+             (long long)c.num_subtris, c.num_subtris * 81.0 * mb, (long long)c.bin_entries, c.bin_entries * 4.0 * mb,
+             (long long)c.tile_entries, c.tile_entries * 4.0 * mb, (long long)c.coarse_units, c.reruns);
+    return CR_OK;
+}
+
+int32_t cr_pipe_count(void) {
+    std::lock_guard<std::mutex> lock(registryMutex());
+    return (int32_t)registry().size();
+}
+
+static void fillInfo(const PipeDesc& p, cr_pipe_info* out) {
+    memset(out, 0, sizeof(*out));
+    strncpy(out->name, p.name, sizeof(out->name) - 1);
+    out->samples_log2 = p.samplesLog2;
+    out->vertex_struct_size = p.vertexStructSize;
+    out->render_mode_flags = p.renderModeFlags;
+    out->profiling_mode = p.profilingMode;
+    strncpy(out->blend_shader_name, p.blendShaderName, sizeof(out->blend_shader_name) - 1);
+    strncpy(out->fragment_shader_name, p.fragmentShaderName, sizeof(out->fragment_shader_name) - 1);
+}
+
+cr_status cr_pipe_info_at(int32_t index, cr_pipe_info* out) {
+    if (!out) return CR_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(registryMutex());
+    if (index < 0 || index >= (int32_t)registry().size()) return CR_ERR_INVALID_ARGUMENT;
+    fillInfo(registry()[index], out);
+    return CR_OK;
+}
+
+cr_status cr_pipe_info_by_name(const char* name, cr_pipe_info* out) {
+    if (!out || !name) return CR_ERR_INVALID_ARGUMENT;
+    const PipeDesc* p = findPipe(name);
+    if (!p) return CR_ERR_NO_PIPE;
+    fillInfo(*p, out);
+    return CR_OK;
+}
+
+}  // extern "C"

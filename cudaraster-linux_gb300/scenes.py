@@ -1,0 +1,197 @@
+"""Seeded synthetic scenes for the benchmark configurations and the tests.
+
+Every scene is a dict with clip-space GouraudVertex records (float32 [N, 8]:
+clipPos xyzw + RGBA colour in [0, 1]), int32 triangle indices [T, 3] and the
+surface description. Vertex positions are produced on the host in float64 and
+rounded once to float32, so the rasterizer and the oracle read identical bits.
+
+  cube      -- the reference demo's 12-triangle cube (test/App.cpp:208-230)
+  soup      -- random triangle soup (lognormal edge length, 50% back-facing)
+  terrain   -- value-noise heightfield grid seen at a grazing angle
+  batch     -- many soups with uneven triangle counts and resolutions
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+# test/App.cpp:210-230
+CUBE_POSITIONS = np.array([
+    [-1, -1, -1], [-1, -1, +1], [-1, +1, -1], [-1, +1, +1],
+    [+1, -1, -1], [+1, -1, +1], [+1, +1, -1], [+1, +1, +1]], dtype=np.float64)
+CUBE_INDICES = np.array([
+    7, 3, 1, 7, 1, 5,
+    7, 5, 6, 6, 5, 4,
+    6, 4, 2, 2, 4, 0,
+    2, 0, 3, 3, 0, 1,
+    3, 7, 6, 3, 6, 2,
+    5, 1, 0, 5, 0, 4], dtype=np.int32).reshape(-1, 3)
+CUBE_COLORS_RGBA8 = np.array([
+    [255, 64, 64, 255], [64, 255, 64, 255], [64, 64, 255, 255], [255, 255, 64, 255],
+    [255, 64, 255, 255], [64, 255, 255, 255], [200, 200, 200, 255], [32, 32, 32, 255]], dtype=np.float64)
+
+
+def perspective(fov_deg: float, aspect: float, near: float, far: float) -> np.ndarray:
+    """OpenGL-style projection; same rows as framework/base/Math.cpp:75-88 with x scaled by 1/aspect."""
+    f = 1.0 / math.tan(math.radians(fov_deg) / 2.0)
+    d = 1.0 / (near - far)
+    return np.array([[f / aspect, 0, 0, 0], [0, f, 0, 0], [0, 0, (near + far) * d, 2 * near * far * d],
+                     [0, 0, -1, 0]], dtype=np.float64)
+
+
+def look_at(eye, target, up=(0.0, 1.0, 0.0)) -> np.ndarray:
+    eye, target, up = (np.asarray(v, dtype=np.float64) for v in (eye, target, up))
+    f = target - eye
+    f /= np.linalg.norm(f)
+    s = np.cross(f, up)
+    s /= np.linalg.norm(s)
+    u = np.cross(s, f)
+    m = np.eye(4)
+    m[0, :3], m[1, :3], m[2, :3] = s, u, -f
+    m[0, 3], m[1, 3], m[2, 3] = -s @ eye, -u @ eye, f @ eye
+    return m
+
+
+def _records(clip: np.ndarray, rgba: np.ndarray) -> np.ndarray:
+    v = np.empty((clip.shape[0], 8), dtype=np.float32)
+    v[:, :4] = clip.astype(np.float32)
+    v[:, 4:] = rgba.astype(np.float32)
+    return v
+
+
+def cube(width: int = 1024, height: int = 768, distance: float = 3.0) -> dict:
+    """Config 1: the demo cube, fov 60, near 0.1, far 100, eye at `distance` from the origin."""
+    eye = np.array([1.0, 1.2, 1.6])
+    eye = eye / np.linalg.norm(eye) * distance
+    mvp = perspective(60.0, width / height, 0.1, 100.0) @ look_at(eye, (0, 0, 0))
+    pos = np.concatenate([CUBE_POSITIONS, np.ones((8, 1))], axis=1)
+    clip = pos @ mvp.T
+    rgba = (CUBE_COLORS_RGBA8.astype(np.float32) / np.float32(255.0)).astype(np.float32)
+    return {"name": "cube", "vertices": _records(clip, rgba), "indices": CUBE_INDICES.copy(),
+            "width": width, "height": height, "samples": 1}
+
+
+def soup(num_tris: int, width: int, height: int, seed: int = 0, median_px: float = 4.0, sigma: float = 1.0,
+         backface_frac: float = 0.5, alpha_range: tuple[float, float] | None = None, samples: int = 1) -> dict:
+    """Config 2: non-indexed random soup. Centroids uniform over the clip-space box
+    (NDC x, y in [-1, 1], z in [-1, 1]), w in [1, 10], lognormal screen-space edge
+    length, random orientation, `backface_frac` reversed winding, RGBA8 colours."""
+    rng = np.random.default_rng(seed)
+    n = num_tris
+    w = rng.uniform(1.0, 10.0, n)
+    cx = rng.uniform(-1.0, 1.0, n)
+    cy = rng.uniform(-1.0, 1.0, n)
+    cz = rng.uniform(-1.0, 1.0, n)
+    edge = np.exp(rng.normal(math.log(median_px), sigma, n))
+    theta = rng.uniform(0.0, 2.0 * math.pi, n)
+    r = edge / math.sqrt(3.0)
+    k = np.arange(3)[None, :]
+    jitter = rng.uniform(-0.35, 0.35, (n, 3))
+    ang = theta[:, None] + (2.0 * math.pi / 3.0) * k + jitter
+    px = r[:, None] * np.cos(ang)
+    py = r[:, None] * np.sin(ang)
+    back = rng.uniform(0.0, 1.0, n) < backface_frac
+    px[back] = px[back][:, ::-1]
+    py[back] = py[back][:, ::-1]
+    nx = cx[:, None] + px * (2.0 / width)
+    ny = cy[:, None] + py * (2.0 / height)
+    nz = np.repeat(cz[:, None], 3, axis=1) + rng.uniform(-0.01, 0.01, (n, 3))
+    nz = np.clip(nz, -1.0, 1.0)
+    ww = np.repeat(w[:, None], 3, axis=1)
+    clip = np.stack([nx * ww, ny * ww, nz * ww, ww], axis=-1).reshape(-1, 4)
+    rgba = rng.integers(0, 256, (3 * n, 4)).astype(np.float32) / np.float32(255.0)
+    if alpha_range is not None:
+        a = rng.uniform(alpha_range[0], alpha_range[1], n)
+        rgba[:, 3] = np.repeat((np.round(a * 255.0) / 255.0).astype(np.float32), 3)
+    idx = np.arange(3 * n, dtype=np.int32).reshape(-1, 3)
+    return {"name": f"soup{n}", "vertices": _records(clip, rgba.astype(np.float32)), "indices": idx,
+            "width": width, "height": height, "samples": samples}
+
+
+def value_noise(nx: int, ny: int, octaves: int = 6, seed: int = 0) -> np.ndarray:
+    """Sum of `octaves` bilinear value-noise layers on an nx x ny grid, in [-1, 1]."""
+    rng = np.random.default_rng(seed)
+    out = np.zeros((ny, nx), dtype=np.float64)
+    amp, total = 1.0, 0.0
+    for o in range(octaves):
+        cells = 4 << o
+        lattice = rng.uniform(-1.0, 1.0, (cells + 2, cells + 2))
+        gx = np.linspace(0.0, cells, nx, endpoint=False)
+        gy = np.linspace(0.0, cells, ny, endpoint=False)
+        ix, iy = gx.astype(np.int64), gy.astype(np.int64)
+        fx, fy = gx - ix, gy - iy
+        fx = fx * fx * (3 - 2 * fx)
+        fy = fy * fy * (3 - 2 * fy)
+        a = lattice[np.ix_(iy, ix)]
+        b = lattice[np.ix_(iy, ix + 1)]
+        c = lattice[np.ix_(iy + 1, ix)]
+        d = lattice[np.ix_(iy + 1, ix + 1)]
+        top = a + (b - a) * fx[None, :]
+        bot = c + (d - c) * fx[None, :]
+        out += amp * (top + (bot - top) * fy[:, None])
+        total += amp
+        amp *= 0.5
+    return out / total
+
+
+def grid_mesh(n: int, seed: int = 0, amplitude: float = 0.2):
+    """n x n vertex heightfield over [-1, 1]^2 (extent 2), heights = amplitude * extent * noise.
+    Returns model-space positions [n*n, 3], colours [n*n, 4] and indices [2(n-1)^2, 3]."""
+    h = value_noise(n, n, 6, seed) * amplitude * 2.0
+    xs = np.linspace(-1.0, 1.0, n)
+    X, Z = np.meshgrid(xs, xs)
+    pos = np.stack([X, h, Z], axis=-1).reshape(-1, 3)
+    t = (h.reshape(-1) / (amplitude * 2.0) + 1.0) * 0.5
+    rgba = np.stack([0.2 + 0.6 * t, 0.5 + 0.3 * (1 - t), 0.25 + 0.2 * t, np.ones_like(t)], axis=-1)
+    rgba = (np.round(rgba * 255.0) / 255.0).astype(np.float32)
+    i = np.arange(n - 1)
+    I, J = np.meshgrid(i, i)
+    v00 = (J * n + I).reshape(-1)
+    v10 = v00 + 1
+    v01 = v00 + n
+    v11 = v01 + 1
+    tris = np.empty((2 * v00.size, 3), dtype=np.int32)
+    tris[0::2] = np.stack([v00, v01, v10], axis=-1)
+    tris[1::2] = np.stack([v10, v01, v11], axis=-1)
+    return pos, rgba, tris
+
+
+def terrain_camera(frame: float = 0.0, width: int = 3840, height: int = 2160, elevation_deg: float = 15.0):
+    """Camera at a grazing angle above the heightfield; `frame` moves it along a closed spline."""
+    t = frame * 2.0 * math.pi / 300.0
+    ex = 1.25 * math.sin(t)
+    ez = 1.25 * math.cos(t)
+    dist = math.hypot(ex, ez)
+    ey = 0.25 + dist * math.tan(math.radians(elevation_deg)) * 0.5
+    target = (0.3 * math.sin(t + 0.7), 0.0, 0.3 * math.cos(t + 0.7))
+    mvp = perspective(60.0, width / height, 0.05, 10.0) @ look_at((ex, ey, ez), target)
+    return mvp
+
+
+def terrain(n: int, width: int, height: int, samples: int = 1, seed: int = 0, frame: float = 0.0) -> dict:
+    """Config 3 (n = 2048, 3840x2160, 4x MSAA) and the config 5 grid (n = 4096)."""
+    pos, rgba, tris = grid_mesh(n, seed)
+    mvp = terrain_camera(frame, width, height)
+    clip = np.concatenate([pos, np.ones((pos.shape[0], 1))], axis=1) @ mvp.T
+    return {"name": f"terrain{n}", "vertices": _records(clip, rgba), "indices": tris,
+            "width": width, "height": height, "samples": samples, "mvp": mvp, "model": pos, "rgba": rgba}
+
+
+BATCH_RESOLUTIONS = [(256, 256), (512, 512), (1024, 768), (1920, 1080)]
+
+
+def batch(count: int = 64, lo: int = 1000, hi: int = 500_000, seed: int = 0, blend_frac: float = 0.5) -> list[dict]:
+    """Config 4: `count` soups, triangle counts log-uniform in [lo, hi], resolutions
+    from BATCH_RESOLUTIONS, `blend_frac` of them alpha-blended (alpha in [0.2, 1])."""
+    rng = np.random.default_rng(seed)
+    scenes = []
+    for i in range(count):
+        n = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+        w, h = BATCH_RESOLUTIONS[int(rng.integers(0, len(BATCH_RESOLUTIONS)))]
+        blended = i < int(round(count * blend_frac))
+        s = soup(n, w, h, seed=seed * 1000 + i + 1, alpha_range=(0.2, 1.0) if blended else None)
+        s["blend"] = "srcover" if blended else "replace"
+        scenes.append(s)
+    order = rng.permutation(count)
+    return [scenes[i] for i in order]

@@ -1,0 +1,194 @@
+/*
+ * cudaraster.h -- C ABI of the GB300 sort-middle rasterizer.
+ *
+ * Every entry point takes plain pointers and sizes (device pointers where
+ * noted) and returns a cr_status. The C++ drop-in classes in
+ * include/cudaraster/CudaRaster.hpp are a header-only layer over this file.
+ *
+ * Reference interface replaced (tcoppex/cudaraster-linux):
+ *   CudaRaster::init                 src/cudaraster/CudaRaster.cpp:98-128      -> cr_create
+ *   CudaRaster::~CudaRaster          src/cudaraster/CudaRaster.cpp:80-94       -> cr_destroy
+ *   CudaRaster::setSurfaces          src/cudaraster/CudaRaster.cpp:132-170     -> cr_set_surfaces
+ *   CudaRaster::deferredClear        src/cudaraster/CudaRaster.cpp:174-179     -> cr_deferred_clear
+ *   CudaRaster::setPixelPipe         src/cudaraster/CudaRaster.cpp:183-216     -> cr_set_pixel_pipe
+ *   CudaRaster::setVertexBuffer      src/cudaraster/CudaRaster.cpp:220-224     -> cr_set_vertex_buffer
+ *   CudaRaster::setIndexBuffer       src/cudaraster/CudaRaster.cpp:228-233     -> cr_set_index_buffer
+ *   CudaRaster::drawTriangles        src/cudaraster/CudaRaster.cpp:237-342     -> cr_draw_triangles
+ *   CudaRaster::getStats             src/cudaraster/CudaRaster.cpp:346-363     -> cr_get_stats
+ *   CudaRaster::getProfilingInfo     src/cudaraster/CudaRaster.cpp:367-497     -> cr_get_profiling_info
+ *   CudaRaster::setDebugParams       src/cudaraster/CudaRaster.hpp:53-67,168   -> cr_set_debug_params
+ *   g_crAtomics read-back            src/cudaraster/CudaRaster.cpp:326         -> cr_get_counters
+ *   CudaModule::getKernel/getGlobal  src/framework/gpu/CudaModule.cpp:161-261  -> cr_pipe_count/cr_pipe_info
+ *   encodeDepth / Vec4f::toABGR      src/cudaraster/cuda/Util.hpp:290-298,
+ *                                    src/framework/base/Math.cpp:41-48         -> cr_encode_depth / cr_color_to_abgr
+ */
+#ifndef CUDARASTER_H
+#define CUDARASTER_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CR_ABI_VERSION 1
+
+typedef enum cr_status {
+    CR_OK = 0,
+    CR_ERR_INVALID_ARGUMENT = 1, /* bad pointer, size, sample count, name ...            */
+    CR_ERR_INVALID_STATE = 2,    /* e.g. drawTriangles before surfaces / pipe are set   */
+    CR_ERR_NO_PIPE = 3,          /* setPixelPipe with an unknown name                    */
+    CR_ERR_PIPE_MISMATCH = 4,    /* pipe sample count differs from the surfaces          */
+    CR_ERR_CAPACITY = 5,         /* a hard limit was exceeded (triangles, viewport ...) */
+    CR_ERR_CUDA = 6,             /* a CUDA runtime call failed (see cr_last_error)       */
+    CR_ERR_TIMEOUT = 7,          /* a device-side bounded wait gave up                   */
+    CR_ERR_OUT_OF_MEMORY = 8,
+    CR_ERR_UNSUPPORTED = 9       /* feature not available in this build                  */
+} cr_status;
+
+/* Render mode flags, as RenderModeFlag_* in src/cudaraster/cuda/PixelPipe.hpp:30-35. */
+#define CR_RENDER_DEPTH 1u
+#define CR_RENDER_LERP  2u
+#define CR_RENDER_QUADS 4u
+
+/* Limits. The reference caps the viewport at 2048 px and subtriangles at 2^24
+ * (Constants.hpp:21, 38); here the viewport may reach 4095 px (snapped vertex
+ * coordinates must stay in S16) and subtriangle slots 2^29 (list entries
+ * hold triangleIndex << 3 | subtriangleIndex in 32 bits). */
+#define CR_MAX_VIEWPORT      4095
+#define CR_MAX_TRIANGLES     ((1 << 29) - 1)
+#define CR_TILE_SIZE_PX      8
+
+typedef struct cr_context cr_context;
+
+/* Per-stage times of the last draw in seconds (CudaRaster.hpp:45-51). */
+typedef struct cr_stats {
+    float setup_time;
+    float bin_time;
+    float coarse_time;
+    float fine_time;
+} cr_stats;
+
+/* Device counters of the last draw (the reference's CRAtomics, PrivateDefs.hpp:123-143),
+ * plus the capacities that were in force and how many reruns the draw took. */
+typedef struct cr_counters {
+    int64_t num_tris;
+    int64_t num_subtris;          /* subtriangle slots used (num_tris + clip extras)  */
+    int64_t bin_entries;          /* (bin, subtriangle) list entries                  */
+    int64_t tile_entries;         /* (tile, subtriangle) list entries                 */
+    int64_t coarse_units;         /* coarse work units                                */
+    int64_t max_subtris;
+    int64_t max_bin_entries;
+    int64_t max_tile_entries;
+    int32_t reruns;               /* overflow-detect-and-rerun iterations of the draw */
+    int32_t overflow;             /* nonzero if the last launch overflowed            */
+    int32_t num_bins;
+    int32_t num_tiles;
+} cr_counters;
+
+/* Static description of a compiled pixel pipe (the reference's PixelPipeSpec,
+ * PrivateDefs.hpp:147-154). */
+typedef struct cr_pipe_info {
+    char     name[64];
+    int32_t  samples_log2;
+    int32_t  vertex_struct_size;
+    uint32_t render_mode_flags;
+    int32_t  profiling_mode;
+    char     blend_shader_name[64];
+    char     fragment_shader_name[64];
+} cr_pipe_info;
+
+/* Debug parameters (CudaRaster.hpp:53-67). Host emulation of stages is not
+ * part of this library: setting any flag returns CR_ERR_UNSUPPORTED. */
+typedef struct cr_debug_params {
+    int32_t emulate_triangle_setup;
+    int32_t emulate_bin_raster;
+    int32_t emulate_coarse_raster;
+    int32_t emulate_fine_raster;
+} cr_debug_params;
+
+/* Tuning knobs (the reference's compile-time CR_* constants turned run-time).
+ * Any value <= 0 keeps the default. Output bits do not depend on them. */
+typedef struct cr_tuning {
+    int32_t bin_log2;             /* tiles per bin side, log2: 3, 4 (default) or 5    */
+    int32_t bin_chunk_tris;       /* triangles per bin-stage work chunk               */
+    int32_t coarse_unit_entries;  /* bin entries per coarse work unit                 */
+    int32_t fine_warps;           /* warps per fine-raster CTA                        */
+    int32_t fine_ctas_per_sm;     /* resident fine CTAs per SM                        */
+} cr_tuning;
+
+/* One scene of a batched draw (cr_draw_batch). All pointers are device pointers. */
+typedef struct cr_instance {
+    const char* pipe;             /* pixel pipe name                                  */
+    void*       color;            /* RGBA8 surface, reference layout                  */
+    void*       depth;            /* DEPTH32 surface, reference layout                */
+    int32_t     width, height, num_samples;
+    const void* vertices;         /* vertex records of the pipe's vertex struct       */
+    const void* indices;          /* int32 triplets                                   */
+    int32_t     num_tris;
+    int32_t     deferred_clear;   /* 1 => clear before drawing                        */
+    uint32_t    clear_color;      /* ABGR8                                            */
+    uint32_t    clear_depth;      /* encoded (cr_encode_depth)                        */
+} cr_instance;
+
+/* ---- Lifecycle ---- */
+cr_status   cr_create(cr_context** out);
+cr_status   cr_destroy(cr_context* ctx);
+const char* cr_status_string(cr_status s);
+const char* cr_last_error(const cr_context* ctx);
+int32_t     cr_abi_version(void);
+
+/* ---- State (CudaRaster.hpp:147-168) ---- */
+/* color / depth: device pointers to surfaces of the reference's layout:
+ * rounded_height rows of (rounded_width * num_samples) 32-bit words, where
+ * rounded_* = size rounded up to 8, and sample i of pixel (x, y) at word
+ * y * (rounded_width * num_samples) + (x / 8) * 8 * num_samples + i * 8 + x % 8. */
+cr_status cr_set_surfaces(cr_context* ctx, void* color, void* depth,
+                          int32_t width, int32_t height, int32_t num_samples);
+cr_status cr_deferred_clear(cr_context* ctx, float r, float g, float b, float a, float depth);
+cr_status cr_deferred_clear_raw(cr_context* ctx, uint32_t abgr, uint32_t encoded_depth);
+cr_status cr_set_pixel_pipe(cr_context* ctx, const char* name);
+cr_status cr_set_vertex_buffer(cr_context* ctx, const void* vertices, int64_t offset_bytes);
+cr_status cr_set_index_buffer(cr_context* ctx, const void* indices, int64_t offset_bytes,
+                              int32_t num_tris);
+cr_status cr_set_tuning(cr_context* ctx, const cr_tuning* tuning);
+cr_status cr_set_debug_params(cr_context* ctx, const cr_debug_params* params);
+/* Initial capacities (elements). Zero keeps the reference's estimates
+ * (CudaRaster.cpp:263-275); undersized values are grown by the rerun loop. */
+cr_status cr_set_capacity(cr_context* ctx, int64_t max_subtris, int64_t max_bin_entries,
+                          int64_t max_tile_entries);
+
+/* ---- Drawing ---- */
+/* Draws the current index buffer on `stream` (a cudaStream_t; NULL = legacy
+ * default stream). Like the reference it checks the device counters after the
+ * draw and reruns with larger queues on overflow, so it synchronises with the
+ * stream before returning. */
+cr_status cr_draw_triangles(cr_context* ctx, void* stream);
+/* Asynchronous variant: no host synchronisation and no rerun. The caller
+ * checks cr_get_counters().overflow after synchronising. */
+cr_status cr_draw_triangles_async(cr_context* ctx, void* stream);
+/* Several independent scenes in one set of launches. */
+cr_status cr_draw_batch(cr_context* ctx, const cr_instance* instances, int32_t count, void* stream);
+cr_status cr_draw_batch_async(cr_context* ctx, const cr_instance* instances, int32_t count, void* stream);
+
+/* ---- Results ---- */
+cr_status cr_get_stats(cr_context* ctx, cr_stats* out);
+cr_status cr_get_counters(cr_context* ctx, cr_counters* out);
+cr_status cr_get_profiling_info(cr_context* ctx, char* buffer, int64_t size);
+
+/* ---- Pipes ---- */
+int32_t   cr_pipe_count(void);
+cr_status cr_pipe_info_at(int32_t index, cr_pipe_info* out);
+cr_status cr_pipe_info_by_name(const char* name, cr_pipe_info* out);
+
+/* ---- Host helpers matching the reference's host arithmetic ---- */
+uint32_t cr_color_to_abgr(float r, float g, float b, float a);   /* Math.cpp:41-48      */
+uint32_t cr_encode_depth(uint32_t depth);                         /* Util.hpp:290-298    */
+uint32_t cr_decode_depth(uint32_t depth);                         /* Util.hpp:302-310    */
+uint32_t cr_clear_depth_from_float(float depth);                  /* CudaRaster.cpp:178  */
+
+#ifdef __cplusplus
+}
+#endif
+#endif

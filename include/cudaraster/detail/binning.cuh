@@ -1,0 +1,88 @@
+// binning.cuh -- conservative triangle-vs-rectangle tests shared by the bin
+// and coarse stages. A triangle is kept for a bin / tile unless its bounding
+// box misses it or one edge has the whole rectangle strictly outside; exact
+// per-sample coverage is decided later by the fine stage, so a kept triangle
+// that covers no sample changes no output bit. The reference makes the same
+// conservative choice with its bbox fast paths and corner tests
+// (BinRaster.inl:208-300, CoarseRaster.inl:299-435).
+#pragma once
+
+#include "device.cuh"
+
+namespace cr {
+
+struct TriGeom {
+    S32 x0, y0, x1, y1, x2, y2;   // header frame: subpixels relative to the viewport centre
+};
+
+__device__ __forceinline__ TriGeom geomFromHeader(uint4 h) {
+    TriGeom g;
+    g.x0 = lo16(h.x); g.y0 = hi16(h.x);
+    g.x1 = lo16(h.y); g.y1 = hi16(h.y);
+    g.x2 = lo16(h.z); g.y2 = hi16(h.z);
+    return g;
+}
+
+// max over the closed rectangle [rx0, rx1] x [ry0, ry1] of (o - P) x d,
+// compared against zero: returns false if the rectangle lies strictly on the
+// outer side of the edge line.
+__device__ __forceinline__ bool edgeTouchesRect(S32 ox, S32 oy, S32 dx, S32 dy, S32 rx0, S32 ry0, S32 rx1, S32 ry1) {
+    S32 px = dy > 0 ? rx0 : rx1;
+    S32 py = dx > 0 ? ry1 : ry0;
+    S64 e = (S64)(ox - px) * dy - (S64)(oy - py) * dx;
+    return e >= 0;
+}
+
+__device__ __forceinline__ bool triTouchesRect(const TriGeom& g, S32 rx0, S32 ry0, S32 rx1, S32 ry1) {
+    return edgeTouchesRect(g.x0, g.y0, g.x1 - g.x0, g.y1 - g.y0, rx0, ry0, rx1, ry1) &&
+           edgeTouchesRect(g.x1, g.y1, g.x2 - g.x1, g.y2 - g.y1, rx0, ry0, rx1, ry1) &&
+           edgeTouchesRect(g.x2, g.y2, g.x0 - g.x2, g.y0 - g.y2, rx0, ry0, rx1, ry1);
+}
+
+// Cells of side 2^cellLog2 subpixels over a grid of gw x gh cells whose
+// origin is the viewport's top-left corner (header frame offset by half the
+// viewport). Calls fn(cx, cy) for every cell the triangle may touch, in
+// row-major order, restricted to [cx0, cx1] x [cy0, cy1].
+template <class Fn>
+__device__ __forceinline__ void forEachCell(const TriGeom& g, S32 halfW, S32 halfH, int cellLog2,
+                                            S32 cx0, S32 cy0, S32 cx1, S32 cy1, Fn fn) {
+    S32 lx = (min3i(g.x0, g.x1, g.x2) + halfW) >> cellLog2;
+    S32 hx = (max3i(g.x0, g.x1, g.x2) + halfW) >> cellLog2;
+    S32 ly = (min3i(g.y0, g.y1, g.y2) + halfH) >> cellLog2;
+    S32 hy = (max3i(g.y0, g.y1, g.y2) + halfH) >> cellLog2;
+    lx = max(lx, cx0); ly = max(ly, cy0);
+    hx = min(hx, cx1); hy = min(hy, cy1);
+    if (lx > hx || ly > hy) return;
+    const bool small = (hx - lx) <= 1 && (hy - ly) <= 1;
+    const S32 cell = 1 << cellLog2;
+    for (S32 cy = ly; cy <= hy; cy++) {
+        for (S32 cx = lx; cx <= hx; cx++) {
+            if (!small) {
+                S32 rx0 = (cx << cellLog2) - halfW, ry0 = (cy << cellLog2) - halfH;
+                if (!triTouchesRect(g, rx0, ry0, rx0 + cell - 1, ry0 + cell - 1)) continue;
+            }
+            fn(cx, cy);
+        }
+    }
+}
+
+// List entry <-> data slot: entry = triangle << 3 | subtriangle, 7 = the
+// triangle's own slot (BinRaster.inl:148-158).
+__device__ __forceinline__ S64 entrySlot(U32 entry, const uint4* triHeader) {
+    U32 tri = entry >> 3, sub = entry & 7;
+    if (sub == 7) return (S64)tri;
+    return (S64)__ldg(&triHeader[tri].w) + sub;
+}
+
+// Warp-level inclusive scan.
+__device__ __forceinline__ S32 warpInclusiveScan(S32 v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        S32 t = __shfl_up_sync(0xFFFFFFFFu, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+}  // namespace cr

@@ -1,0 +1,156 @@
+"""ctypes wrapper of the CPU oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, as the checker. The product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "liboracle.so"
+REF_LIB = HERE / "_ref" / "libcrref.so"
+
+DEPTH, LERP, QUADS = 1, 2, 4
+BLENDS = {"replace": 0, "srcover": 1, "additive": 2, "depthonly": 3}
+SHADERS = {"gouraud": 0, "red": 1, "trihash": 2, "deriv": 3}
+
+
+class Pipe(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("samples_log2", C.c_int32),
+                ("render_mode", C.c_uint32), ("blend", C.c_int32), ("shader", C.c_int32),
+                ("vertex_stride", C.c_int32), ("deferred_clear", C.c_int32), ("clear_color", C.c_uint32),
+                ("clear_depth", C.c_uint32)]
+
+
+class OrStats(C.Structure):
+    _fields_ = [("num_subtris", C.c_int64), ("num_clipped", C.c_int64), ("num_fragments", C.c_int64),
+                ("zmin_violations", C.c_int64), ("tile_entries", C.c_int64)]
+
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            subprocess.run(["make", "-C", str(HERE), "liboracle.so"], check=True, capture_output=True)
+        lib = C.CDLL(str(LIB))
+        lib.or_setup.restype = C.c_int64
+        lib.or_setup.argtypes = [C.POINTER(Pipe), C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
+                                 C.c_void_p, C.c_int64]
+        lib.or_render.restype = C.c_int
+        lib.or_render.argtypes = [C.POINTER(Pipe), C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
+                                  C.c_int, C.POINTER(OrStats)]
+        for name, res, args in [
+            ("or_to_abgr", C.c_uint32, [C.c_float] * 4), ("or_host_to_abgr", C.c_uint32, [C.c_float] * 4),
+            ("or_encode_depth", C.c_uint32, [C.c_uint32]), ("or_decode_depth", C.c_uint32, [C.c_uint32]),
+            ("or_clear_depth", C.c_uint32, [C.c_float]),
+            ("or_blend", C.c_uint32, [C.c_int, C.c_uint32, C.c_uint32, C.POINTER(C.c_int)]),
+            ("or_select_flips", C.c_uint32, [C.c_int32, C.c_int32]),
+            ("or_select_msaa_centroid", C.c_int, [C.c_int, C.c_uint32]),
+            ("or_centroid_lut", None, [C.c_int, C.c_void_p]),
+            ("or_setup_pleq", None, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_int, C.c_void_p]),
+            ("or_clip_triangle", C.c_int, [C.c_void_p] * 6),
+            ("or_cover8x8_exact", C.c_uint64, [C.c_int32] * 4),
+            ("or_cover8x8_conservative", C.c_uint64, [C.c_int32] * 4),
+            ("or_cover_msaa", C.c_uint32, [C.c_int] + [C.c_int32] * 4),
+            ("or_triangle_pixel_coverage", C.c_uint64, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
+            ("or_triangle_sample_coverage", C.c_uint32, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
+            ("or_compute_barys", None, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]),
+            ("or_find_bit", C.c_int, [C.c_uint64, C.c_int, C.c_int]),
+            ("or_fragment", C.c_uint32, [C.POINTER(Pipe), C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
+                                         C.c_uint32]),
+            ("or_perspective", None, [C.c_float, C.c_float, C.c_float, C.c_void_p]),
+            ("or_f32_to_s32_sat", C.c_int32, [C.c_float]), ("or_f32_to_u32_sat", C.c_uint32, [C.c_float]),
+            ("or_f32_to_u32_sat_rmi", C.c_uint32, [C.c_float]), ("or_f32_to_s64", C.c_int64, [C.c_float]),
+            ("or_f32_to_u32_rz", C.c_uint32, [C.c_float]),
+        ]:
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def make_pipe(width, height, samples=1, flags=DEPTH | LERP, blend="replace", shader="gouraud", stride=32,
+              clear=None) -> Pipe:
+    p = Pipe()
+    p.width, p.height = width, height
+    p.samples_log2 = int(samples).bit_length() - 1
+    p.render_mode = flags
+    p.blend = BLENDS[blend]
+    p.shader = SHADERS[shader]
+    p.vertex_stride = stride
+    if clear is not None:
+        p.deferred_clear = 1
+        p.clear_color, p.clear_depth = clear
+    return p
+
+
+def surface_shape(width, height, samples):
+    return ((height + 7) & ~7, ((width + 7) & ~7) * samples)
+
+
+def render(pipe: Pipe, vertices: np.ndarray, indices: np.ndarray, color=None, depth=None, threads: int = 0):
+    """Renders in place into color/depth (uint32 arrays of surface_shape), returns (color, depth, stats)."""
+    lib = load()
+    shape = surface_shape(pipe.width, pipe.height, 1 << pipe.samples_log2)
+    color = np.zeros(shape, np.uint32) if color is None else np.ascontiguousarray(color, dtype=np.uint32)
+    depth = np.zeros(shape, np.uint32) if depth is None else np.ascontiguousarray(depth, dtype=np.uint32)
+    v = np.ascontiguousarray(vertices, dtype=np.float32)
+    i = np.ascontiguousarray(indices, dtype=np.int32)
+    st = OrStats()
+    lib.or_render(C.byref(pipe), v.ctypes.data, i.ctypes.data, i.shape[0], color.ctypes.data, depth.ctypes.data,
+                  int(threads), C.byref(st))
+    return color, depth, {f: getattr(st, f) for f, _ in OrStats._fields_}
+
+
+def setup(pipe: Pipe, vertices: np.ndarray, indices: np.ndarray, max_subtris: int | None = None):
+    """Triangle setup outputs: (tri_subtris[T], headers[S,4], data[S,16], used)."""
+    lib = load()
+    v = np.ascontiguousarray(vertices, dtype=np.float32)
+    i = np.ascontiguousarray(indices, dtype=np.int32)
+    t = i.shape[0]
+    ms = max_subtris or (t * 7 + 16)
+    sub = np.zeros(t, np.uint8)
+    hdr = np.zeros((ms, 4), np.uint32)
+    dat = np.zeros((ms, 16), np.uint32)
+    used = lib.or_setup(C.byref(pipe), v.ctypes.data, i.ctypes.data, t, sub.ctypes.data, hdr.ctypes.data,
+                        dat.ctypes.data, ms)
+    return sub, hdr, dat, used
+
+
+def ref_available() -> bool:
+    return REF_LIB.exists()
+
+
+def load_ref():
+    """The reference's own device code compiled for the host (oracle/_ref, built only where the
+    reference sources exist)."""
+    lib = C.CDLL(str(REF_LIB))
+    lib.ref_triangle_setup.restype = C.c_int
+    lib.ref_triangle_setup.argtypes = [C.c_int, C.c_uint, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                       C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+    for n in ["ref_cover8x8_exact_ref", "ref_cover8x8_exact_fast", "ref_cover8x8_conservative_ref",
+              "ref_cover8x8_conservative_fast", "ref_cover8x8_exact_noLUT", "ref_triangle_pixel_coverage"]:
+        getattr(lib, n).restype = C.c_ulonglong
+    lib.ref_triangle_pixel_coverage.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]
+    lib.ref_triangle_sample_coverage.restype = C.c_uint
+    lib.ref_triangle_sample_coverage.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]
+    for n in ["ref_to_abgr", "ref_host_to_abgr"]:
+        getattr(lib, n).restype = C.c_uint
+        getattr(lib, n).argtypes = [C.c_float] * 4
+    for n in ["ref_encode_depth", "ref_decode_depth", "ref_select_flips", "ref_blend", "ref_coverMSAA_ref",
+              "ref_coverMSAA_fast", "ref_gouraud_fragment"]:
+        getattr(lib, n).restype = C.c_uint
+    lib.ref_gouraud_fragment.argtypes = [C.c_int, C.c_uint, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                         C.c_int, C.c_uint]
+    lib.ref_setup_pleq.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_int, C.c_void_p]
+    lib.ref_perspective.argtypes = [C.c_float, C.c_float, C.c_float, C.c_void_p]
+    return lib
