@@ -1,0 +1,316 @@
+"""Benchmark of the GB300 rasterizer on the plain-path-at-scale configuration:
+a 1M-triangle random soup at 1920x1080, 1 sample per pixel, Gouraud shading,
+depth LESS, opaque (seeded synthetic input).
+
+One step = one drawTriangles() of the whole soup through the C ABI (the
+reference's plain path: setup -> bin -> coarse -> fine, then the host reads
+the overflow counters). `value` is device-timed with CUDA events on the
+drawing stream, inputs resident in HBM, L2 flushed (256 MiB write) before
+every step. `e2e` times the same draw with the inputs copied from pinned host
+memory and the framebuffer copied back inside the timed region.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+With --impl reference the CPU restatement of the reference pipeline (the
+oracle, OpenMP over all host cores) renders the same scene; under torchrun
+only rank 0 runs it.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+PKG = "cudaraster-linux_gb300"
+
+METRIC = "frames/s & Mtri/s on 1 GB300: batched+predicted vs plain, bit-exact framebuffers"
+WORKLOAD = {"workload": "plain path at scale: 1M-triangle random soup, 1920x1080, 1 spp, Gouraud, depth LESS, opaque",
+            "num_tris": 1_000_000, "width": 1920, "height": 1080, "samples": 1, "pipe": "PixelPipe_gouraud",
+            "seed": 2, "l2": "flushed before every step (256 MiB write)"}
+
+
+def load_scene():
+    scenes = importlib.import_module(PKG + ".scenes")
+    return scenes.soup(WORKLOAD["num_tris"], WORKLOAD["width"], WORKLOAD["height"], seed=WORKLOAD["seed"])
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(sc, budget_s: float = 12.0, min_frames: int = 1):
+    """The oracle (CPU restatement of the reference pipeline, OpenMP) on the same scene."""
+    from oracle import oracle as orc
+    pkg = importlib.import_module(PKG)
+    threads = os.cpu_count() or 1
+    pipe = orc.make_pipe(sc["width"], sc["height"], 1, orc.DEPTH | orc.LERP, "replace", "gouraud",
+                         clear=(pkg.color_to_abgr(0.2, 0.4, 0.8, 1.0), pkg.clear_depth_from_float(1.0)))
+    frames, t0, out = 0, time.perf_counter(), None
+    while True:
+        out = orc.render(pipe, sc["vertices"], sc["indices"], threads=threads)
+        frames += 1
+        if frames >= min_frames and time.perf_counter() - t0 >= budget_s:
+            break
+    el = time.perf_counter() - t0
+    return {"value": frames / el, "unit": "frames/s", "cores": threads, "kind": "port",
+            "sample": f"{frames} full frame(s) of the same 1M-triangle scene in {el:.1f} s",
+            "mtri_per_s": frames * sc["indices"].shape[0] / el / 1e6}, out
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    sc = load_scene()
+    steps = max(1, args.steps)
+    for _ in range(max(0, min(args.warmup, 1))):
+        cpu_baseline(sc, budget_s=0.0)
+    cb, _ = cpu_baseline(sc, budget_s=0.0, min_frames=steps)
+    line = {"impl": "reference", "metric": METRIC, "value": round(cb["value"], 4), "unit": "frames/s",
+            "n_gpus": world, "steps": steps, "warmup": args.warmup, "ms_per_step": round(1000.0 / cb["value"], 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+int32",
+            "data": "synthetic (seeded)", "config": WORKLOAD, "mtri_per_s": round(cb["mtri_per_s"], 3),
+            "cpu_baseline": cb, "e2e": {"value": round(cb["value"], 4), "unit": "frames/s",
+                                         "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": 0}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-frames", type=int, default=0,
+                    help="only draw this many frames of the workload (for ncu captures), print nothing else")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    import torch.distributed as dist
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    pkg = importlib.import_module(PKG)
+    sc = load_scene()
+    T = sc["indices"].shape[0]
+    W, H = sc["width"], sc["height"]
+
+    cr = pkg.CudaRaster()
+    cr.init()
+    color = pkg.CudaSurface((W, H), pkg.CudaSurface.FORMAT_RGBA8, 1)
+    depth = pkg.CudaSurface((W, H), pkg.CudaSurface.FORMAT_DEPTH32, 1)
+    cr.setSurfaces(color, depth)
+    cr.setPixelPipe(None, WORKLOAD["pipe"])
+    verts = torch.from_numpy(sc["vertices"]).cuda()
+    idx = torch.from_numpy(sc["indices"]).cuda()
+    cr.setVertexBuffer(verts, 0)
+    cr.setIndexBuffer(idx, 0, T)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def draw():
+        cr.deferredClear((0.2, 0.4, 0.8, 1.0), 1.0)
+        cr.drawTriangles(stream)
+
+    if args.profile_frames > 0:
+        for _ in range(args.profile_frames):
+            draw()
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_frames": args.profile_frames, "counters": cr.getCounters()}))
+        return
+
+    for _ in range(max(3, args.warmup)):
+        draw()
+    torch.cuda.synchronize()
+
+    # ---- device-timed steps
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    stage = np.zeros(4)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            flush.fill_(i & 0xFF)
+            starts[i].record(stream)
+            draw()
+            ends[i].record(stream)
+            s = cr.getStats()
+            stage += [s.setupTime, s.binTime, s.coarseTime, s.fineTime]
+        torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * args.steps / (total_ms / 1e3)
+    stage_ms = stage / args.steps * 1e3
+    counters = cr.getCounters()
+
+    # ---- end-to-end through the C ABI with host buffers
+    hv = torch.from_numpy(sc["vertices"]).pin_memory()
+    hi = torch.from_numpy(sc["indices"]).pin_memory()
+    hc = torch.empty_like(color.tensor, device="cpu").pin_memory()
+    hd = torch.empty_like(depth.tensor, device="cpu").pin_memory()
+    dv = torch.empty_like(verts)
+    di = torch.empty_like(idx)
+    cr.setVertexBuffer(dv, 0)
+    cr.setIndexBuffer(di, 0, T)
+
+    def e2e_step():
+        dv.copy_(hv, non_blocking=True)
+        di.copy_(hi, non_blocking=True)
+        draw()
+        hc.copy_(color.tensor, non_blocking=True)
+        hd.copy_(depth.tensor, non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_ms = []
+    for i in range(args.steps):
+        flush.fill_(i & 0xFF)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        e2e_step()
+        b.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms.append(a.elapsed_time(b))
+    e2e_total = sum(e2e_ms)
+    if world > 1:
+        t = torch.tensor([e2e_total], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    e2e_value = world * args.steps / (e2e_total / 1e3)
+    h2d = hv.numel() * 4 + hi.numel() * 4
+    d2h = (hc.numel() + hd.numel()) * 4
+
+    # ---- roofline of the dominant stage (stage events bracket its kernels)
+    peak, peak_kind = peaks()
+    names = ["setup", "bin", "coarse", "fine"]
+    dom = int(np.argmax(stage_ms))
+    V = sc["vertices"].shape[0]
+    # Algorithmic bytes per launch of each stage (one frame):
+    #   setup : index 12 B + clipPos 16 B x 3 vertices read, subtri byte + header 16 B + data 64 B written per triangle
+    #   bin   : subtri count + header per triangle read twice (count, scatter), 4 B per bin entry written
+    #   coarse: 4 B entry + 16 B header per bin entry read twice, 4 B per tile entry written
+    #   fine  : per tile entry 4 B + header 16 B + data 64 B, colour+depth of every sample written once
+    N = ((W + 7) // 8 * 8) * ((H + 7) // 8 * 8)
+    alg = {
+        "setup": T * (12 + 48 + 1 + 16 + 64),
+        "bin": T * 2 * (1 + 16) + counters["bin_entries"] * 4,
+        "coarse": counters["bin_entries"] * 2 * (4 + 16) + counters["tile_entries"] * 4,
+        "fine": counters["tile_entries"] * (4 + 16 + 64) + N * 8,
+    }
+    achieved = alg[names[dom]] / (stage_ms[dom] / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": names[dom], "achieved": round(achieved, 1), "peak": peak,
+                "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                "traffic": None, "alg_bytes_per_launch": int(alg[names[dom]]),
+                "stage_ms": {n: round(float(m), 4) for n, m in zip(names, stage_ms)}}
+    b_alg = 12 * T + 32 * V + 8 * N
+    frame_frac = b_alg / (ms_per_step / 1e3) / 1e9 / peak
+
+    line = {"metric": METRIC, "value": round(value, 3), "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+int32", "data": "synthetic (seeded)",
+            "config": WORKLOAD, "mtri_per_s": round(T * value / 1e6, 2),
+            "frame_roofline_frac": round(frame_frac, 4), "frame_alg_bytes": int(b_alg),
+            "e2e": {"value": round(e2e_value, 3), "unit": "frames/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_total / args.steps, 4)},
+            "roofline": roofline, "clocks": clk.summary(),
+            "gpu_launches": 8 * args.steps, "counters": counters}
+    if rank == 0 and not args.no_cpu_baseline:
+        cb, (rc, rd, st) = cpu_baseline(sc)
+        gc = color.download().numpy().astype(np.uint32)
+        gd = depth.download().numpy().astype(np.uint32)
+        line["cpu_baseline"] = cb
+        line["bit_exact_vs_oracle"] = bool((gc == rc).all() and (gd == rd).all())
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

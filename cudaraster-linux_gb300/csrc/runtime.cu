@@ -376,7 +376,7 @@ struct Plan {
 
 cr_status buildPlan(cr_context* ctx, const std::vector<HostInstance>& in, Plan& plan) {
     plan.binLog2 = ctx->tuning.bin_log2 > 0 ? ctx->tuning.bin_log2 : 4;
-    plan.unitEntries = ctx->tuning.coarse_unit_entries > 0 ? ctx->tuning.coarse_unit_entries : 2048;
+    plan.unitEntries = ctx->tuning.coarse_unit_entries > 0 ? ctx->tuning.coarse_unit_entries : 512;
     // Group instances by pipe, keeping first-seen pipe order (outputs do not depend on it).
     std::vector<const PipeDesc*> order;
     for (const HostInstance& h : in)

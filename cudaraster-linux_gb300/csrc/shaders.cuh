@@ -36,4 +36,7 @@ public:
     }
 };
 
+template <> struct FragmentShaderTraits<FragmentShader_passthrough> { static constexpr bool mayDiscard = false; };
+template <> struct FragmentShaderTraits<TriHashShader> { static constexpr bool mayDiscard = false; };
+
 }  // namespace FW

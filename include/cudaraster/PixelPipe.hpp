@@ -232,6 +232,20 @@ public:
     __device__ __forceinline__ void run(void) { m_writeColor = false; }
 };
 
+// ---------------------------------------------------------- shader traits
+// Compile-time facts the fine stage uses to pick its algorithm. With depth
+// testing on, a blend shader that ignores the destination and a fragment
+// shader that never discards, the colour and depth of every sample depend
+// only on the front-most covering fragment (earliest in submission order on
+// ties), so the fine stage resolves visibility first and shades each sample's
+// winner once. The defaults are the safe ones; specialise them for your own
+// shaders when the facts hold.
+template <class BS> struct BlendShaderTraits { static constexpr bool needsDst = true; };
+template <> struct BlendShaderTraits<BlendReplace> { static constexpr bool needsDst = false; };
+template <> struct BlendShaderTraits<BlendDepthOnly> { static constexpr bool needsDst = false; };
+template <class FS> struct FragmentShaderTraits { static constexpr bool mayDiscard = true; };
+template <> struct FragmentShaderTraits<GouraudShader> { static constexpr bool mayDiscard = false; };
+
 // Profiling modes (PixelPipe.hpp:208-213). Only the default mode (per-stage
 // events + device counters) exists here.
 #define ProfilingMode_Default 0

@@ -66,6 +66,33 @@ __device__ __forceinline__ void forEachCell(const TriGeom& g, S32 halfW, S32 hal
     }
 }
 
+// Cell range of a triangle's bounding box, clamped to [cx0, cx1] x [cy0, cy1].
+struct CellBox {
+    S32 lx, ly, hx, hy;
+    __device__ __forceinline__ S32 count() const { return (lx > hx || ly > hy) ? 0 : (hx - lx + 1) * (hy - ly + 1); }
+    __device__ __forceinline__ bool small() const { return (hx - lx) <= 1 && (hy - ly) <= 1; }
+};
+
+__device__ __forceinline__ CellBox cellBox(const TriGeom& g, S32 halfW, S32 halfH, int cellLog2,
+                                           S32 cx0, S32 cy0, S32 cx1, S32 cy1) {
+    CellBox b;
+    b.lx = max((min3i(g.x0, g.x1, g.x2) + halfW) >> cellLog2, cx0);
+    b.hx = min((max3i(g.x0, g.x1, g.x2) + halfW) >> cellLog2, cx1);
+    b.ly = max((min3i(g.y0, g.y1, g.y2) + halfH) >> cellLog2, cy0);
+    b.hy = min((max3i(g.y0, g.y1, g.y2) + halfH) >> cellLog2, cy1);
+    return b;
+}
+
+// Is cell (cx, cy) of box b touched by the triangle? (bbox shortcut for boxes
+// of at most 2x2 cells, as the reference's bin/coarse fast paths.)
+__device__ __forceinline__ bool cellTouched(const TriGeom& g, const CellBox& b, S32 cx, S32 cy, S32 halfW, S32 halfH,
+                                            int cellLog2) {
+    if (b.small()) return true;
+    const S32 cell = 1 << cellLog2;
+    S32 rx0 = (cx << cellLog2) - halfW, ry0 = (cy << cellLog2) - halfH;
+    return triTouchesRect(g, rx0, ry0, rx0 + cell - 1, ry0 + cell - 1);
+}
+
 // List entry <-> data slot: entry = triangle << 3 | subtriangle, 7 = the
 // triangle's own slot (BinRaster.inl:148-158).
 __device__ __forceinline__ S64 entrySlot(U32 entry, const uint4* triHeader) {

@@ -3,23 +3,31 @@
 // One warp owns one 8x8 tile at a time (persistent warps pulling tiles from a
 // counter, as FineRaster.inl:534-552). The tile's colour and depth live in the
 // warp's shared memory for the whole tile. Its triangle list is consumed in
-// batches of 32:
-//   1. lane i fetches entry i: header, data slot, early-Z against the tile's
-//      current maximum depth (FineRaster.inl:229-240), edge functions at the
-//      tile origin;
-//   2. the 32 lanes, each owning two pixels, evaluate every triangle of the
-//      batch and ballot a 64-bit pixel coverage mask per triangle;
-//   3. covered pixels are compacted into passes of 32 fragments in
-//      submission order (FineRaster.inl:625-731);
-//   4. each fragment is depth-tested, shaded and blended. Fragments of the
-//      same pass that hit the same pixel are grouped with __match_any_sync
-//      and applied one rank at a time in lane order, which is submission
-//      order. This replaces the reference's reliance on lock-step warps for
-//      same-address shared-memory races (FineRaster.inl:433-495, 758-851),
-//      which is undefined on sm_70 and later.
+// batches of 32; lane i fetches entry i (header, data slot, early-Z against
+// the tile's current maximum depth as FineRaster.inl:229-240, edge functions
+// at the tile origin). Then one of two algorithms runs, chosen at compile time:
+//
+// Ordered path (any blend shader, discard, quads):
+//   coverage masks per triangle (small triangles by their own lane, large ones
+//   by the 32 pixel-owning lanes with ballots), covered pixels compacted into
+//   passes of 32 fragments in submission order (FineRaster.inl:625-731), then
+//   depth test, shading and blending per fragment. Fragments of one pass that
+//   hit the same pixel are grouped with __match_any_sync and applied one rank
+//   at a time in lane order, which is submission order. This replaces the
+//   reference's reliance on lock-step warps for same-address shared-memory
+//   races (FineRaster.inl:433-495, 758-851), undefined on sm_70 and later.
+//
+// Visibility path (depth test on, blend shader that ignores the destination,
+//   fragment shader that never discards): the final colour and depth of a
+//   sample are those of its front-most covering fragment, the earliest one in
+//   submission order on equal depth -- the same result as applying every
+//   fragment in order with a LESS test. Each sample keeps a 64-bit key
+//   (depth << 32 | list position + 1) that fragments lower with atomicMin;
+//   after the list, every sample's winner is shaded once.
+//
 // MSAA keeps every sample of the tile in shared memory (reference layout:
 // sample i of pixel x at word i * 8 + x of the tile row) and shades once per
-// pixel at the centroid of the covered samples.
+// (pixel, triangle) at the centroid of the triangle's covered samples.
 #pragma once
 
 #include "../PixelPipe.hpp"
@@ -27,16 +35,22 @@
 
 namespace cr {
 
+constexpr int kFineMaxThreads = 256;
+// Triangles whose pixel box inside the tile has at most this many pixels get
+// their coverage from their own lane; larger ones from the whole warp.
+constexpr int kFineSelfPixels = 12;
+
 template <int S>
 struct FineWarpSmem {
     static constexpr int kTileWords = 64 << S;
     U32 color[kTileWords];
     U32 depth[kTileWords];
-    S32 E[3][32];      // edge functions at the tile's pixel (0, 0) centre, bias folded in
-    S32 A[3][32];      // per-subpixel x step (-dy)
-    S32 B[3][32];      // per-subpixel y step (+dx)
-    U32 td[16][32];    // triangle data slots (CRTriangleData words)
-    S32 tri[32];       // triangle index within the draw
+    U64 key[kTileWords];   // visibility keys (visibility path only)
+    S32 E[3][32];          // edge functions at the tile's pixel (0, 0) centre, bias folded in
+    S32 A[3][32];          // per-subpixel x step (-dy)
+    S32 B[3][32];          // per-subpixel y step (+dx)
+    U32 td[16][32];        // triangle data slots (CRTriangleData words)
+    S32 tri[32];           // triangle index within the draw
     U32 covLo[32];
     U32 covHi[32];
     S32 fragEnd[32];
@@ -80,15 +94,122 @@ __device__ __forceinline__ S32 clampEdge(S64 e) {
     return (S32)(e > lim ? lim : (e < -lim ? -lim : e));
 }
 
-constexpr int kFineMaxThreads = 256;
+// Edge functions of a header relative to the tile's pixel (0, 0) centre:
+// edges (v0, v1 - v0), (v1, v2 - v1), (v0, v0 - v2) as FineRaster.inl:251-275,
+// bias of the fill rule (Util.inl:100) folded in. A sample at subpixel offset
+// q from that centre is covered iff E[k] + A[k] * q.x + B[k] * q.y >= 0 for
+// all k (the offsets stay below 2^8 and |A|, |B| below 2^17, so clamping E to
+// +-2^30 keeps every sign).
+struct TileEdges {
+    S32 E[3], A[3], B[3];
+    S32 minX, maxX, minY, maxY;   // vertex box relative to the pixel (0, 0) centre
+};
+
+__device__ __forceinline__ TileEdges tileEdges(uint4 h, S32 cx0, S32 cy0) {
+    TileEdges t;
+    S32 vx[3] = {lo16(h.x) - cx0, lo16(h.y) - cx0, lo16(h.z) - cx0};
+    S32 vy[3] = {hi16(h.x) - cy0, hi16(h.y) - cy0, hi16(h.z) - cy0};
+    const int oi[3] = {0, 1, 0};
+    S32 ddx[3] = {vx[1] - vx[0], vx[2] - vx[1], vx[0] - vx[2]};
+    S32 ddy[3] = {vy[1] - vy[0], vy[2] - vy[1], vy[0] - vy[2]};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        S64 e = (S64)vx[oi[k]] * ddy[k] - (S64)vy[oi[k]] * ddx[k];
+        if (ddy[k] > 0 || (ddy[k] == 0 && ddx[k] <= 0)) e -= 1;
+        t.E[k] = clampEdge(e);
+        t.A[k] = -ddy[k];
+        t.B[k] = ddx[k];
+    }
+    t.minX = min3i(vx[0], vx[1], vx[2]);
+    t.maxX = max3i(vx[0], vx[1], vx[2]);
+    t.minY = min3i(vy[0], vy[1], vy[2]);
+    t.maxY = max3i(vy[0], vy[1], vy[2]);
+    return t;
+}
+
+__device__ __forceinline__ bool edgesCover(const S32* E, const S32* A, const S32* B, S32 qx, S32 qy) {
+    return (E[0] + A[0] * qx + B[0] * qy >= 0) && (E[1] + A[1] * qx + B[1] * qy >= 0) &&
+           (E[2] + A[2] * qx + B[2] * qy >= 0);
+}
+
+// Exact sample mask of pixel (px, py) of the tile.
+template <int S>
+__device__ __forceinline__ U32 sampleMaskOf(const S32* E, const S32* A, const S32* B, S32 px, S32 py) {
+    U32 m = 0;
+#pragma unroll
+    for (int i = 0; i < (1 << S); i++)
+        if (edgesCover(E, A, B, (px << kSubpixelLog2) + sampleOffsetX(S, i), (py << kSubpixelLog2) + sampleOffsetY(S, i)))
+            m |= 1u << i;
+    return m;
+}
+
+// Depth of sample i of pixel (X, Y) (FineRaster.inl:695, 1047, 1096).
+template <int S>
+__device__ __forceinline__ U32 sampleDepth(U32 zx, U32 zy, U32 zb, U32 X, U32 Y, int i) {
+    if (S == 0) return zx * X + zy * Y + zb;
+    return zx * (U32)msaaPatternX(S, i) + zy * (U32)i + (((zx * X + zy * Y) << S) + zb);
+}
+
+// Pixel box [bx0, bx1] x [by0, by1] of the tile that can hold covered samples.
+template <int S>
+__device__ __forceinline__ bool pixelBox(const TileEdges& t, S32& bx0, S32& bx1, S32& by0, S32& by1) {
+    const S32 pad = (S == 0) ? 0 : 8;
+    bx0 = max(0, (t.minX - pad + 15) >> kSubpixelLog2);
+    bx1 = min(7, (t.maxX + pad) >> kSubpixelLog2);
+    by0 = max(0, (t.minY - pad + 15) >> kSubpixelLog2);
+    by1 = min(7, (t.maxY + pad) >> kSubpixelLog2);
+    return bx0 <= bx1 && by0 <= by1;
+}
+
+// Runs the fragment shader of triangle data td (16 words) at pixel (X, Y).
+template <class FS, int S, U32 F>
+__device__ __forceinline__ U32 shadeFragment(const U32* td, S32 triIdx, S32 X, S32 Y, U32 sampleMask,
+                                             const float4* verts, S32 stride4, volatile F32* shared, U32 laneMask,
+                                             bool& discard) {
+    FS fs;
+    fs.m_triIdx = triIdx;
+    fs.m_vertIdx = FW::Vec3i((S32)td[13], (S32)td[14], (S32)td[15]);
+    fs.m_pixelPos = FW::Vec2i(X, Y);
+    fs.m_vertexBytes = stride4 * 16;
+    fs.m_shared = shared;
+    fs.m_vertices = verts;
+    fs.m_laneMask = laneMask;
+    fs.m_color = 0xFF0000FFu;
+    fs.m_discard = false;
+    if (!(F & kRenderLerp)) {
+        // Interpolation disabled => varyings at the last vertex (FineRaster.inl:71-81).
+        fs.m_center = FW::Vec3f(0.0f, 0.0f, 1.0f);
+        fs.m_centerDX = FW::Vec3f(0.0f);
+        fs.m_centerDY = FW::Vec3f(0.0f);
+        fs.m_centroid = fs.m_center;
+        fs.m_centroidDX = fs.m_centerDX;
+        fs.m_centroidDY = fs.m_centerDY;
+    } else {
+        computeBarys<S>(fs.m_center, fs.m_centerDX, fs.m_centerDY, td + 4, td + 7, td + 10, (X * 2 + 1) << S,
+                        (Y * 2 + 1) << S);
+        if (S == 0) {
+            fs.m_centroid = fs.m_center;
+            fs.m_centroidDX = fs.m_centerDX;
+            fs.m_centroidDY = fs.m_centerDY;
+        } else {
+            U32 c = centroidCode(S, sampleMask);
+            computeBarys<S>(fs.m_centroid, fs.m_centroidDX, fs.m_centroidDY, td + 4, td + 7, td + 10,
+                            (X << (S + 1)) + (S32)(c & 0xF), (Y << (S + 1)) + (S32)(c >> 4));
+        }
+    }
+    fs.run();
+    discard = fs.m_discard;
+    return fs.m_color;
+}
 
 template <class V, class FS, class BS, int S, U32 F>
 __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int group, S32 tileBegin, S32 tileEnd) {
     constexpr int NS = 1 << S;
     constexpr int TW = 64 << S;
     constexpr bool kDepth = (F & kRenderDepth) != 0;
-    constexpr bool kLerp = (F & kRenderLerp) != 0;
     constexpr bool kQuads = (F & kRenderQuads) != 0;
+    constexpr bool kVisibility = kDepth && !kQuads && !FW::BlendShaderTraits<BS>::needsDst &&
+                                 !FW::FragmentShaderTraits<FS>::mayDiscard;
     extern __shared__ __align__(16) unsigned char fineSmemRaw[];
     FineWarpSmem<S>& sm = reinterpret_cast<FineWarpSmem<S>*>(fineSmemRaw)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
@@ -143,9 +264,16 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
         const S32 stride4 = __ldg(&in->stride4);
         const float4* verts = (const float4*)__ldg((const unsigned long long*)&in->vertices);
 
+        if constexpr (kVisibility) {
+            for (int w = lane; w < TW; w += 32) sm.key[w] = (U64)sm.depth[w] << 32;
+            __syncwarp();
+        }
+
         for (S32 batch = 0; batch < count; batch += 32) {
-            // 1. Fetch one triangle per lane.
+            // ---- 1. One triangle per lane.
             bool valid = batch + lane < count;
+            bool self = false;     // small triangle: this lane handles all of it
+            U32 myLo = 0, myHi = 0;
             if (valid) {
                 U32 entry = __ldg(&d.tileList[start + batch + lane]);
                 U32 tri = entry >> 3, sub = entry & 7;
@@ -153,62 +281,139 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
                 uint4 h = __ldg(&d.triHeader[slot]);
                 if (kDepth && (h.w & 0xFFFFF000u) >= tileZMax) valid = false;
                 if (valid) {
-                    S32 vx[3] = {lo16(h.x), lo16(h.y), lo16(h.z)};
-                    S32 vy[3] = {hi16(h.x), hi16(h.y), hi16(h.z)};
-                    // Edges (v0, v1 - v0), (v1, v2 - v1), (v0, v0 - v2) as FineRaster.inl:251-275.
-                    const int oi[3] = {0, 1, 0};
-                    S32 ddx[3] = {vx[1] - vx[0], vx[2] - vx[1], vx[0] - vx[2]};
-                    S32 ddy[3] = {vy[1] - vy[0], vy[2] - vy[1], vy[0] - vy[2]};
+                    const TileEdges te = tileEdges(h, cx0, cy0);
 #pragma unroll
                     for (int k = 0; k < 3; k++) {
-                        S64 e = (S64)(vx[oi[k]] - cx0) * ddy[k] - (S64)(vy[oi[k]] - cy0) * ddx[k];
-                        if (ddy[k] > 0 || (ddy[k] == 0 && ddx[k] <= 0)) e -= 1;  // Util.inl:100
-                        sm.E[k][lane] = clampEdge(e);
-                        sm.A[k][lane] = -ddy[k];
-                        sm.B[k][lane] = ddx[k];
+                        sm.E[k][lane] = te.E[k];
+                        sm.A[k][lane] = te.A[k];
+                        sm.B[k][lane] = te.B[k];
                     }
-                    const uint4* td = &d.triData[slot * 4];
-                    uint4 q0 = __ldg(&td[0]), q1 = __ldg(&td[1]), q2 = __ldg(&td[2]), q3 = __ldg(&td[3]);
+                    const uint4* tdp = &d.triData[slot * 4];
+                    uint4 q0 = __ldg(&tdp[0]);
                     sm.td[0][lane] = q0.x; sm.td[1][lane] = q0.y; sm.td[2][lane] = q0.z; sm.td[3][lane] = q0.w;
-                    sm.td[4][lane] = q1.x; sm.td[5][lane] = q1.y; sm.td[6][lane] = q1.z; sm.td[7][lane] = q1.w;
-                    sm.td[8][lane] = q2.x; sm.td[9][lane] = q2.y; sm.td[10][lane] = q2.z; sm.td[11][lane] = q2.w;
-                    sm.td[12][lane] = q3.x; sm.td[13][lane] = q3.y; sm.td[14][lane] = q3.z; sm.td[15][lane] = q3.w;
-                    sm.tri[lane] = (S32)((S64)tri - triBase);
+                    if constexpr (!kVisibility) {
+                        uint4 q1 = __ldg(&tdp[1]), q2 = __ldg(&tdp[2]), q3 = __ldg(&tdp[3]);
+                        sm.td[4][lane] = q1.x; sm.td[5][lane] = q1.y; sm.td[6][lane] = q1.z; sm.td[7][lane] = q1.w;
+                        sm.td[8][lane] = q2.x; sm.td[9][lane] = q2.y; sm.td[10][lane] = q2.z; sm.td[11][lane] = q2.w;
+                        sm.td[12][lane] = q3.x; sm.td[13][lane] = q3.y; sm.td[14][lane] = q3.z; sm.td[15][lane] = q3.w;
+                        sm.tri[lane] = (S32)((S64)tri - triBase);
+                    }
+                    S32 bx0, bx1, by0, by1;
+                    if (!pixelBox<S>(te, bx0, bx1, by0, by1)) {
+                        self = true;  // no pixel of the tile can be covered
+                    } else if ((bx1 - bx0 + 1) * (by1 - by0 + 1) <= kFineSelfPixels) {
+                        self = true;
+                        const U64 order = (U64)(U32)(batch + lane + 1);
+                        for (S32 py = by0; py <= by1; py++) {
+                            for (S32 px = bx0; px <= bx1; px++) {
+                                const U32 X = (U32)(tx * 8 + px), Y = (U32)(ty * 8 + py);
+                                if constexpr (kVisibility) {
+                                    const U32 smask = sampleMaskOf<S>(te.E, te.A, te.B, px, py);
+#pragma unroll
+                                    for (int i = 0; i < NS; i++) {
+                                        if (!(smask >> i & 1)) continue;
+                                        const int idx = py * 8 * NS + i * 8 + px;
+                                        const U64 k = ((U64)sampleDepth<S>(q0.x, q0.y, q0.z, X, Y, i) << 32) | order;
+                                        if (k < sm.key[idx]) atomicMin((unsigned long long*)&sm.key[idx], (unsigned long long)k);
+                                    }
+                                } else {
+                                    const S32 qx = px << kSubpixelLog2, qy = py << kSubpixelLog2;
+                                    bool c = true;
+#pragma unroll
+                                    for (int k = 0; k < 3; k++) {
+                                        S32 slack = (S == 0) ? 0 : (abs(te.A[k]) + abs(te.B[k])) << (kSubpixelLog2 - 1);
+                                        c = c && (te.E[k] + te.A[k] * qx + te.B[k] * qy + slack >= 0);
+                                    }
+                                    if (kDepth && S == 0 && !kQuads && c) c = (q0.x * X + q0.y * Y + q0.z) < sm.depth[py * 8 + px];
+                                    if (c) {
+                                        const int bit = py * 8 + px;
+                                        if (bit < 32) myLo |= 1u << bit; else myHi |= 1u << (bit - 32);
+                                    }
+                                }
+                            }
+                        }
+                    }
                 }
             }
             __syncwarp();
-            U32 validMask = __ballot_sync(0xFFFFFFFFu, valid);
+            const U32 coopMask = __ballot_sync(0xFFFFFFFFu, valid && !self);
 
-            // 2. Pixel coverage per triangle, two pixels per lane.
-            const S32 qx = (lane & 7) << kSubpixelLog2;
-            const S32 qy0 = (lane >> 3) << kSubpixelLog2;
-            const S32 qy1 = qy0 + (4 << kSubpixelLog2);
-            U32 myLo = 0, myHi = 0;
-            for (U32 m = validMask; m; m &= m - 1) {
-                const int j = __ffs(m) - 1;
-                bool c0 = true, c1 = true;
+            // ---- 2. Large triangles, two pixels per lane.
+            const S32 px = lane & 7, py0 = lane >> 3, py1 = py0 + 4;
+            const U32 pX = (U32)(tx * 8 + px), pY0 = (U32)(ty * 8 + py0), pY1 = pY0 + 4;
+            if constexpr (kVisibility) {
+                for (U32 m = coopMask; m; m &= m - 1) {
+                    const int j = __ffs(m) - 1;
+                    const S32 E[3] = {sm.E[0][j], sm.E[1][j], sm.E[2][j]};
+                    const S32 A[3] = {sm.A[0][j], sm.A[1][j], sm.A[2][j]};
+                    const S32 B[3] = {sm.B[0][j], sm.B[1][j], sm.B[2][j]};
+                    const U32 zx = sm.td[0][j], zy = sm.td[1][j], zb = sm.td[2][j];
+                    const U64 order = (U64)(U32)(batch + j + 1);
 #pragma unroll
-                for (int k = 0; k < 3; k++) {
-                    S32 e = sm.E[k][j], a = sm.A[k][j], b = sm.B[k][j];
-                    S32 base = e + a * qx;
-                    S32 slack = (S == 0) ? 0 : (abs(a) + abs(b)) << (kSubpixelLog2 - 1);
-                    c0 = c0 && (base + b * qy0 + slack >= 0);
-                    c1 = c1 && (base + b * qy1 + slack >= 0);
+                    for (int half = 0; half < 2; half++) {
+                        const S32 pyy = half ? py1 : py0;
+                        const U32 Y = half ? pY1 : pY0;
+                        const U32 smask = sampleMaskOf<S>(E, A, B, px, pyy);
+#pragma unroll
+                        for (int i = 0; i < NS; i++) {
+                            if (!(smask >> i & 1)) continue;
+                            const int idx = pyy * 8 * NS + i * 8 + px;
+                            const U64 k = ((U64)sampleDepth<S>(zx, zy, zb, pX, Y, i) << 32) | order;
+                            if (k < sm.key[idx]) sm.key[idx] = k;
+                        }
+                    }
                 }
-                U32 lo = __ballot_sync(0xFFFFFFFFu, c0);
-                U32 hi = __ballot_sync(0xFFFFFFFFu, c1);
-                if (kQuads) {
-                    // quadCoverage (FineRaster.inl:401-406): bit of the quad's top-left pixel.
-                    U64 c = ((U64)hi << 32) | lo;
-                    c |= c >> 1;
-                    c |= c >> 8;
-                    c &= 0x0055005500550055ull;
-                    lo = (U32)c; hi = (U32)(c >> 32);
+                __syncwarp();
+                // Exact current depth maximum for the next batch's early Z.
+                U32 z = 0;
+                for (int w = lane; w < TW; w += 32) z = max(z, (U32)(sm.key[w] >> 32));
+                tileZMax = __reduce_max_sync(0xFFFFFFFFu, z);
+                continue;
+            } else {
+                // Single-sample depth of this lane's two pixels at the start of
+                // the batch: a fragment that fails against it fails in
+                // submission order too (depths only decrease).
+                U32 curZ0 = 0, curZ1 = 0;
+                if (kDepth && S == 0 && !kQuads) {
+                    curZ0 = sm.depth[lane];
+                    curZ1 = sm.depth[lane + 32];
                 }
-                if (lane == j) { myLo = lo; myHi = hi; }
+                const S32 qx = px << kSubpixelLog2, qy0 = py0 << kSubpixelLog2, qy1 = py1 << kSubpixelLog2;
+                for (U32 m = coopMask; m; m &= m - 1) {
+                    const int j = __ffs(m) - 1;
+                    bool c0 = true, c1 = true;
+#pragma unroll
+                    for (int k = 0; k < 3; k++) {
+                        S32 e = sm.E[k][j], a = sm.A[k][j], b = sm.B[k][j];
+                        S32 base = e + a * qx;
+                        S32 slack = (S == 0) ? 0 : (abs(a) + abs(b)) << (kSubpixelLog2 - 1);
+                        c0 = c0 && (base + b * qy0 + slack >= 0);
+                        c1 = c1 && (base + b * qy1 + slack >= 0);
+                    }
+                    if (kDepth && S == 0 && !kQuads) {
+                        const U32 zx = sm.td[0][j], zy = sm.td[1][j], zb = sm.td[2][j];
+                        const U32 z0 = zx * pX + zy * pY0 + zb;
+                        c0 = c0 && (z0 < curZ0);
+                        c1 = c1 && (z0 + zy * 4u < curZ1);
+                    }
+                    U32 lo = __ballot_sync(0xFFFFFFFFu, c0);
+                    U32 hi = __ballot_sync(0xFFFFFFFFu, c1);
+                    if (lane == j) { myLo = lo; myHi = hi; }
+                }
             }
-            // 3. Fragment compaction in submission order.
-            S32 pop = (__popc(myLo) + __popc(myHi)) * (kQuads ? 4 : 1);
+            if (kQuads) {
+                // quadCoverage (FineRaster.inl:401-406): bit of the quad's top-left pixel.
+                U64 c = ((U64)myHi << 32) | myLo;
+                c |= c >> 1;
+                c |= c >> 8;
+                c &= 0x0055005500550055ull;
+                myLo = (U32)c;
+                myHi = (U32)(c >> 32);
+            }
+            if (!valid) { myLo = 0; myHi = 0; }
+
+            // ---- 3. Fragment compaction in submission order.
+            const S32 pop = (__popc(myLo) + __popc(myHi)) * (kQuads ? 4 : 1);
             S32 inc = pop;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
@@ -236,42 +441,35 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
                         if (sm.fragEnd[mid] > f) hi = mid; else lo = mid + 1;
                     }
                     j = lo;
-                    const S32 k = f - (sm.fragEnd[j] - (S32)((__popc(sm.covLo[j]) + __popc(sm.covHi[j])) * (kQuads ? 4 : 1)));
+                    const U32 cl = sm.covLo[j], ch = sm.covHi[j];
+                    const S32 k = f - (sm.fragEnd[j] - (S32)((__popc(cl) + __popc(ch)) * (kQuads ? 4 : 1)));
                     if (kQuads) {
-                        int qbit = nthSetBit64(sm.covLo[j], sm.covHi[j], k >> 2);
+                        int qbit = nthSetBit64(cl, ch, k >> 2);
                         pixel = qbit + (k & 1) + ((k & 2) << 2);  // findFragment, FineRaster.inl:417-427
                     } else {
-                        pixel = nthSetBit64(sm.covLo[j], sm.covHi[j], k);
+                        pixel = nthSetBit64(cl, ch, k);
                     }
-                    const S32 px = pixel & 7, py = pixel >> 3;
-                    // Exact sample coverage.
-#pragma unroll
-                    for (int i = 0; i < NS; i++) {
-                        const S32 sx = (px << kSubpixelLog2) + sampleOffsetX(S, i);
-                        const S32 sy = (py << kSubpixelLog2) + sampleOffsetY(S, i);
-                        bool c = true;
-#pragma unroll
-                        for (int e = 0; e < 3; e++) c = c && (sm.E[e][j] + sm.A[e][j] * sx + sm.B[e][j] * sy >= 0);
-                        if (c) sampleMask |= 1u << i;
+                    const S32 fx = pixel & 7, fy = pixel >> 3;
+                    if (S == 0 && !kQuads) {
+                        sampleMask = 1;  // single-sample masks are exact
+                    } else {
+                        const S32 E[3] = {sm.E[0][j], sm.E[1][j], sm.E[2][j]};
+                        const S32 A[3] = {sm.A[0][j], sm.A[1][j], sm.A[2][j]};
+                        const S32 B[3] = {sm.B[0][j], sm.B[1][j], sm.B[2][j]};
+                        sampleMask = sampleMaskOf<S>(E, A, B, fx, fy);
                     }
                     covered = sampleMask != 0;
                     if (!kQuads && !covered) act = false;
-                    // Depth at the samples (FineRaster.inl:695, 1047, 1096).
-                    const U32 X = (U32)(tx * 8 + px), Y = (U32)(ty * 8 + py);
+                    const U32 X = (U32)(tx * 8 + fx), Y = (U32)(ty * 8 + fy);
                     if (kDepth) {
                         const U32 zx = sm.td[0][j], zy = sm.td[1][j], zb = sm.td[2][j];
                         bool anyPass = false;
-                        if (S == 0) {
-                            dz[0] = zx * X + zy * Y + zb;
-                        } else {
-                            const U32 zbase = ((zx * X + zy * Y) << S) + zb;
+                        const int rowBase = fy * 8 * NS + fx;
 #pragma unroll
-                            for (int i = 0; i < NS; i++) dz[i] = zx * (U32)msaaPatternX(S, i) + zy * (U32)i + zbase;
-                        }
-                        const int rowBase = py * 8 * NS + px;
-#pragma unroll
-                        for (int i = 0; i < NS; i++)
+                        for (int i = 0; i < NS; i++) {
+                            dz[i] = sampleDepth<S>(zx, zy, zb, X, Y, i);
                             if ((sampleMask >> i & 1) && dz[i] < sm.depth[rowBase + i * 8]) anyPass = true;
+                        }
                         if (!kQuads && !anyPass) act = false;
                         if (kQuads && !anyPass) covered = false;
                     }
@@ -281,43 +479,11 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
                 U32 src = 0;
                 bool discard = true;
                 if (act) {
-                    const S32 px = pixel & 7, py = pixel >> 3;
-                    const S32 X = tx * 8 + px, Y = ty * 8 + py;
-                    FS fs;
-                    fs.m_triIdx = sm.tri[j];
-                    fs.m_vertIdx = FW::Vec3i((S32)sm.td[13][j], (S32)sm.td[14][j], (S32)sm.td[15][j]);
-                    fs.m_pixelPos = FW::Vec2i(X, Y);
-                    fs.m_vertexBytes = stride4 * 16;
-                    fs.m_shared = sm.shared;
-                    fs.m_vertices = verts;
-                    fs.m_laneMask = shadeMask;
-                    fs.m_color = 0xFF0000FFu;
-                    fs.m_discard = false;
-                    if (!kLerp) {
-                        fs.m_center = FW::Vec3f(0.0f, 0.0f, 1.0f);
-                        fs.m_centerDX = FW::Vec3f(0.0f);
-                        fs.m_centerDY = FW::Vec3f(0.0f);
-                        fs.m_centroid = fs.m_center;
-                        fs.m_centroidDX = fs.m_centerDX;
-                        fs.m_centroidDY = fs.m_centerDY;
-                    } else {
-                        U32 w[3] = {sm.td[4][j], sm.td[5][j], sm.td[6][j]};
-                        U32 u[3] = {sm.td[7][j], sm.td[8][j], sm.td[9][j]};
-                        U32 v[3] = {sm.td[10][j], sm.td[11][j], sm.td[12][j]};
-                        computeBarys<S>(fs.m_center, fs.m_centerDX, fs.m_centerDY, w, u, v, (X * 2 + 1) << S, (Y * 2 + 1) << S);
-                        if (S == 0) {
-                            fs.m_centroid = fs.m_center;
-                            fs.m_centroidDX = fs.m_centerDX;
-                            fs.m_centroidDY = fs.m_centerDY;
-                        } else {
-                            U32 c = centroidCode(S, sampleMask);
-                            computeBarys<S>(fs.m_centroid, fs.m_centroidDX, fs.m_centroidDY, w, u, v,
-                                            (X << (S + 1)) + (S32)(c & 0xF), (Y << (S + 1)) + (S32)(c >> 4));
-                        }
-                    }
-                    fs.run();
-                    src = fs.m_color;
-                    discard = fs.m_discard;
+                    U32 td[16];
+#pragma unroll
+                    for (int q = 0; q < 16; q++) td[q] = sm.td[q][j];
+                    src = shadeFragment<FS, S, F>(td, sm.tri[j], tx * 8 + (pixel & 7), ty * 8 + (pixel >> 3), sampleMask,
+                                                  verts, stride4, sm.shared, shadeMask, discard);
                 }
                 // ROP: same-pixel fragments of this pass applied in lane order.
                 const bool rop = act && covered && !discard;
@@ -329,8 +495,8 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
                     const int maxGroup = __reduce_max_sync(0xFFFFFFFFu, rop ? __popc(peers) : 0);
                     for (int r = 0; r < maxGroup; r++) {
                         if (rop && rank == r) {
-                            const S32 px = pixel & 7, py = pixel >> 3;
-                            const int rowBase = py * 8 * NS + px;
+                            const S32 fx = pixel & 7, fy = pixel >> 3;
+                            const int rowBase = fy * 8 * NS + fx;
                             BS bs;
 #pragma unroll
                             for (int i = 0; i < NS; i++) {
@@ -341,7 +507,7 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
                                     sm.depth[idx] = dz[i];
                                 }
                                 bs.m_triIdx = sm.tri[j];
-                                bs.m_pixelPos = FW::Vec2i(tx * 8 + px, ty * 8 + py);
+                                bs.m_pixelPos = FW::Vec2i(tx * 8 + fx, ty * 8 + fy);
                                 bs.m_sampleIdx = i;
                                 bs.m_src = src;
                                 bs.m_dst = sm.color[idx];
@@ -359,6 +525,60 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
                 U32 z = 0;
                 for (int w = lane; w < TW; w += 32) z = max(z, sm.depth[w]);
                 tileZMax = __reduce_max_sync(0xFFFFFFFFu, z);
+            }
+            __syncwarp();
+        }
+
+        if constexpr (kVisibility) {
+            // ---- Resolve: shade every (pixel, winning triangle) once.
+            for (int p = lane; p < 64; p += 32) {
+                const S32 px = p & 7, py = p >> 3;
+                const int rowBase = py * 8 * NS + px;
+                U32 done = 0;
+                for (int i0 = 0; i0 < NS; i0++) {
+                    if (done >> i0 & 1) continue;
+                    const U64 k0 = sm.key[rowBase + i0 * 8];
+                    const U32 order = (U32)k0;
+                    if (order == 0) continue;  // no fragment passed the depth test here
+                    // Samples won by the same fragment.
+                    U32 won = 0;
+#pragma unroll
+                    for (int i = 0; i < NS; i++)
+                        if ((U32)sm.key[rowBase + i * 8] == order) won |= 1u << i;
+                    done |= won;
+                    const U32 entry = __ldg(&d.tileList[start + (S32)order - 1]);
+                    const U32 tri = entry >> 3, sub = entry & 7;
+                    const S64 slot = (sub == 7) ? (S64)tri : (S64)__ldg(&d.triHeader[tri].w) + sub;
+                    U32 smask = 1;
+                    if (S != 0) {
+                        const TileEdges te = tileEdges(__ldg(&d.triHeader[slot]), cx0, cy0);
+                        smask = sampleMaskOf<S>(te.E, te.A, te.B, px, py);
+                    }
+                    const uint4* tdp = &d.triData[slot * 4];
+                    uint4 q0 = __ldg(&tdp[0]), q1 = __ldg(&tdp[1]), q2 = __ldg(&tdp[2]), q3 = __ldg(&tdp[3]);
+                    const U32 td[16] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w,
+                                        q2.x, q2.y, q2.z, q2.w, q3.x, q3.y, q3.z, q3.w};
+                    bool discard;
+                    const S32 X = tx * 8 + px, Y = ty * 8 + py;
+                    const U32 src = shadeFragment<FS, S, F>(td, (S32)((S64)tri - triBase), X, Y, smask, verts, stride4,
+                                                            sm.shared, 0u, discard);
+                    BS bs;
+#pragma unroll
+                    for (int i = 0; i < NS; i++) {
+                        if (!(won >> i & 1)) continue;
+                        const int idx = rowBase + i * 8;
+                        sm.depth[idx] = (U32)(sm.key[idx] >> 32);
+                        bs.m_triIdx = (S32)((S64)tri - triBase);
+                        bs.m_pixelPos = FW::Vec2i(X, Y);
+                        bs.m_sampleIdx = i;
+                        bs.m_src = src;
+                        bs.m_dst = sm.color[idx];
+                        bs.m_color = 0xFF0000FFu;
+                        bs.m_writeColor = true;
+                        bs.run();
+                        if (bs.m_writeColor) sm.color[idx] = bs.m_color;
+                    }
+                }
             }
             __syncwarp();
         }
