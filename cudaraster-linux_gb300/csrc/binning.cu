@@ -502,11 +502,10 @@ cudaError_t launchBinning(const DrawDev& d, int maxBins, int numSMs, cudaStream_
         configured = true;
     }
     const int tpb = 1 << (2 * d.binLog2);
-    if (d.totalChunks > 0) {
-        binCountKernel<<<d.totalChunks, kBinThreads, sizeof(S32) * maxBins, stream>>>(d);
-        binScanKernel<<<d.totalBins, kBinThreads, 0, stream>>>(d);
-        binScatterKernel<<<d.totalChunks, kBinThreads, binScatterSmem(maxBins), stream>>>(d);
-    }
+    // binScan also runs for a draw without triangles: it zeroes the bin counts.
+    if (d.totalChunks > 0) binCountKernel<<<d.totalChunks, kBinThreads, sizeof(S32) * maxBins, stream>>>(d);
+    binScanKernel<<<d.totalBins, kBinThreads, 0, stream>>>(d);
+    if (d.totalChunks > 0) binScatterKernel<<<d.totalChunks, kBinThreads, binScatterSmem(maxBins), stream>>>(d);
     if (evCoarse) cudaEventRecord(evCoarse, stream);
     const int coarseGrid = numSMs * 3;
     coarseCountKernel<<<coarseGrid, kBinThreads, sizeof(S32) * tpb, stream>>>(d);

@@ -56,7 +56,8 @@ def init_surfaces(sc: dict, samples: int, seed: int | None):
             rng.integers(0, 2**32, shape, dtype=np.uint64).astype(np.uint32))
 
 
-def gpu_render(pipe: str, sc: dict, clear=None, color=None, depth=None, cr=None, tuning=None, capacity=None):
+def gpu_render(pipe: str, sc: dict, clear=None, color=None, depth=None, cr=None, tuning=None, capacity=None,
+               num_tris=None):
     """Returns (color, depth, counters, stats). clear=(abgr, encoded depth) or None."""
     import torch
     p = pkg()
@@ -81,7 +82,7 @@ def gpu_render(pipe: str, sc: dict, clear=None, color=None, depth=None, cr=None,
     if clear is not None:
         cr._check(cr._lib.cr_deferred_clear_raw(cr._ctx, clear[0], clear[1]))
     cr.setVertexBuffer(verts, 0)
-    cr.setIndexBuffer(idx, 0, idx.shape[0])
+    cr.setIndexBuffer(idx, 0, idx.shape[0] if num_tris is None else num_tris)
     cr.drawTriangles()
     torch.cuda.synchronize()
     gc = cs.download().numpy().astype(np.uint32)

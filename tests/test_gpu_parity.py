@@ -64,3 +64,15 @@ def test_clipping_heavy(cuda):
     rc, rd, st = oracle_render("PixelPipe_gouraud", sc, clear)
     assert st["num_clipped"] > 0
     assert_same(gc, gd, rc, rd, "clipping")
+
+
+def test_empty_draw_clears(cuda):
+    """A draw without triangles still applies the deferred clear to every tile."""
+    sc = pkg_mod("scenes").soup(10, 64, 40, seed=1)
+    c0, d0 = init_surfaces(sc, 1, seed=3)
+    clear = clear_of((0.5, 0.25, 0.125, 1.0), 0.5)
+    gc, gd, _, _ = gpu_render("PixelPipe_gouraud", sc, clear, c0.copy(), d0.copy(), num_tris=0)
+    empty = dict(sc, indices=sc["indices"][:0])
+    rc, rd, _ = oracle_render("PixelPipe_gouraud", empty, clear, c0.copy(), d0.copy())
+    assert_same(gc, gd, rc, rd, "empty draw")
+    assert (gc == clear[0]).all() and (gd == clear[1]).all()
