@@ -44,6 +44,11 @@ const PipeDesc* findPipe(const char* name) {
 }
 }  // namespace
 
+namespace cr {
+// Pipe lookup for other translation units of the library.
+const PipeDesc* findRegisteredPipe(const char* name) { return findPipe(name); }
+}  // namespace cr
+
 extern "C" void cr_register_pipe(const cr::PipeDesc* desc) {
     std::lock_guard<std::mutex> lock(registryMutex());
     for (PipeDesc& p : registry())

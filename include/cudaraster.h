@@ -172,6 +172,24 @@ cr_status cr_draw_triangles_async(cr_context* ctx, void* stream);
 cr_status cr_draw_batch(cr_context* ctx, const cr_instance* instances, int32_t count, void* stream);
 cr_status cr_draw_batch_async(cr_context* ctx, const cr_instance* instances, int32_t count, void* stream);
 
+/* No counterpart in the reference. The same draw as cr_draw_triangles for
+ * callers that may not allocate memory while they run (a host application
+ * that owns a fixed memory budget, a real-time loop where cudaMalloc would
+ * stall the frame, a plugin that only receives device pointers): no context,
+ * no cudaMalloc/cudaFree, no pinned host buffers. The intermediate queues
+ * live in one static array of about 13 MiB compiled into this library, held
+ * by every GPU that loads it until the process exits, and shared by every
+ * call: calls that overlap on the GPU race, so order them on one stream.
+ * Limits: num_tris <= 65536, width and height <= 1024, fixed queue sizes;
+ * larger draws return CR_ERR_CAPACITY (surfaces untouched) with a message in
+ * `error` (may be NULL). The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) with that device current; make it
+ * before any stream capture. Synchronises with `stream` before returning. */
+cr_status cr_draw_triangles_static(const char* pipe, void* color, void* depth, int32_t width, int32_t height,
+                                   int32_t num_samples, const void* vertices, const void* indices,
+                                   int32_t num_tris, int32_t deferred_clear, uint32_t clear_color,
+                                   uint32_t clear_depth, void* stream, char* error, int64_t error_size);
+
 /* ---- Results ---- */
 cr_status cr_get_stats(cr_context* ctx, cr_stats* out);
 cr_status cr_get_counters(cr_context* ctx, cr_counters* out);
