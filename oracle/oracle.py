@@ -153,4 +153,17 @@ def load_ref():
                                          C.c_int, C.c_uint]
     lib.ref_setup_pleq.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_int, C.c_void_p]
     lib.ref_perspective.argtypes = [C.c_float, C.c_float, C.c_float, C.c_void_p]
+    lib.ref_compute_barys.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+    lib.ref_centroid_lut.argtypes = [C.c_int, C.c_void_p]
+    lib.ref_clip_triangle.restype = C.c_int
+    lib.ref_clip_triangle.argtypes = [C.c_void_p] * 6
+    lib.ref_blend.argtypes = [C.c_int, C.c_uint, C.c_uint, C.POINTER(C.c_int)]
+    for n in ["ref_cover8x8_exact_ref", "ref_cover8x8_exact_fast", "ref_cover8x8_conservative_ref",
+              "ref_cover8x8_conservative_fast", "ref_cover8x8_exact_noLUT"]:
+        getattr(lib, n).argtypes = [C.c_int] * 4
+    lib.ref_coverMSAA_ref.argtypes = [C.c_int] * 5
+    lib.ref_coverMSAA_fast.argtypes = [C.c_int] * 5
+    lib.ref_encode_depth.argtypes = [C.c_uint]
+    lib.ref_decode_depth.argtypes = [C.c_uint]
+    lib.ref_select_flips.argtypes = [C.c_int, C.c_int]
     return lib
