@@ -27,7 +27,7 @@ namespace cr {
 constexpr int kBinThreads = 512;
 constexpr int kBinWarps = kBinThreads / 32;
 constexpr int kMaxSubtrisPerTri = 7;
-constexpr int kSmallCells = 4;
+constexpr int kSmallCells = 8;
 
 // Exclusive block scan over kBinThreads values; returns the exclusive prefix,
 // total in *total. scratch >= kBinWarps + 1 ints.
@@ -109,8 +109,12 @@ __device__ __forceinline__ void visitRound(RoundShared& rs, bool valid, const Tr
         const BigItem& it = rs.big[b];
         const S32 w = it.box.hx - it.box.lx + 1;
         const S32 cnt = it.box.count();
+        // Cell c of the box is (c % w, c / w); the quotient is taken in
+        // binary32, exact here because c < 2^11 and w <= 2^5.
+        const F32 invW = 1.0f / (F32)w;
         for (S32 c = lane; c < cnt; c += 32) {
-            S32 cx = it.box.lx + c % w, cy = it.box.ly + c / w;
+            const S32 q = (S32)(((F32)c + 0.5f) * invW);
+            const S32 cx = it.box.lx + (c - q * w), cy = it.box.ly + q;
             if (cellTouched(it.g, it.box, cx, cy, gr.halfW, gr.halfH, gr.cellLog2)) fn(cellIndex(gr, cx, cy), it.who, it.entry);
         }
     }
@@ -148,7 +152,7 @@ __device__ __forceinline__ ItemRound expandRound(const DrawDev& d, S64 r0, S64 t
 // ------------------------------------------------------------------ bin
 
 // One CTA per chunk: counts the chunk's entries per bin.
-__global__ void __launch_bounds__(kBinThreads) binCountKernel(DrawDev d) {
+__global__ void __launch_bounds__(kBinThreads, 2) binCountKernel(DrawDev d) {
     extern __shared__ S32 s_count[];
     __shared__ RoundShared rs;
     __shared__ U32 s_items[kBinThreads * kMaxSubtrisPerTri];
@@ -268,7 +272,7 @@ __device__ __forceinline__ void scatterRound(RoundShared& rs, bool valid, const 
 // round of up to 512 subtriangles the rank of an entry inside its bin is the
 // number of earlier items (lower warp, then lower lane) that touch the same
 // bin, taken from per-warp ballot masks.
-__global__ void __launch_bounds__(kBinThreads) binScatterKernel(DrawDev d) {
+__global__ void __launch_bounds__(kBinThreads, 2) binScatterKernel(DrawDev d) {
     extern __shared__ S32 smem[];
     __shared__ RoundShared rs;
     __shared__ U32 s_items[kBinThreads * kMaxSubtrisPerTri];
@@ -350,7 +354,7 @@ __device__ __forceinline__ Grid tileGrid(const UnitInfo& ui, int binLog2) {
 }
 
 // Persistent CTAs over coarse units: per-unit tile counts.
-__global__ void __launch_bounds__(kBinThreads) coarseCountKernel(DrawDev d) {
+__global__ void __launch_bounds__(kBinThreads, 2) coarseCountKernel(DrawDev d) {
     extern __shared__ S32 s_count[];
     __shared__ RoundShared rs;
     __shared__ int s_inst;
@@ -440,7 +444,7 @@ __global__ void __launch_bounds__(kBinThreads) coarseScanKernel(DrawDev d) {
 
 // Persistent CTAs over coarse units: writes tile list entries, ranked per
 // 512-entry round by per-warp ballot masks over the tiles of the bin.
-__global__ void __launch_bounds__(kBinThreads) coarseScatterKernel(DrawDev d) {
+__global__ void __launch_bounds__(kBinThreads, 2) coarseScatterKernel(DrawDev d) {
     extern __shared__ S32 smem[];
     __shared__ RoundShared rs;
     __shared__ int s_inst;

@@ -124,10 +124,58 @@ __device__ __forceinline__ float4 lerpClip(float4 o, float4 a, float4 b, F32 bu,
                        fadd(fadd(o.z, fmul(a.z, bu)), fmul(b.z, bv)), fadd(fadd(o.w, fmul(a.w, bu)), fmul(b.w, bv)));
 }
 
+// Clip path of triangleSetupImpl (TriangleSetup.inl:326-412), out of line so
+// the common path keeps its registers.
+template <int S, U32 F>
+__device__ __noinline__ void setupClipped(const DrawDev& d, S64 gt, int3 vidx, float4 v0, float4 v1, float4 v2,
+                                          S32 width, S32 height) {
+    int2 d1, d2;
+    S64 area;
+    float4 ov0 = v0;
+    float4 od1 = make_float4(fsub(v1.x, v0.x), fsub(v1.y, v0.y), fsub(v1.z, v0.z), fsub(v1.w, v0.w));
+    float4 od2 = make_float4(fsub(v2.x, v0.x), fsub(v2.y, v0.y), fsub(v2.z, v0.z), fsub(v2.w, v0.w));
+    F32 bary[18];
+    int numVerts = clipTriangle(bary, &ov0.x, &v1.x, &v2.x, &od1.x, &od2.x);
+    float4 c0 = lerpClip(ov0, od1, od2, bary[0], bary[1]);
+    float4 c1 = lerpClip(ov0, od1, od2, bary[2], bary[3]);
+    float4 tc1 = c1;
+
+    int numSubtris = 0;
+    for (int i = 2; i < numVerts; i++) {
+        float4 c2 = lerpClip(ov0, od1, od2, bary[i * 2], bary[i * 2 + 1]);
+        SnapOut sn = snapTriangle(c0, c1, c2, width, height);
+        if (prepareTriangle<S>(sn, width, height, d1, d2, area) == 0) numSubtris++;
+        c1 = c2;
+    }
+    d.triSubtris[gt] = (uint8_t)numSubtris;
+
+    S64 base = gt;
+    if (numSubtris > 1) {
+        base = d.totalTris + atomicAdd(&d.counters->extraSubtris, numSubtris);
+        d.triHeader[gt].w = (U32)base;
+        if (base + numSubtris > d.maxSubtris) {
+            atomicOr(&d.counters->overflow, kOverflowSubtris);
+            numVerts = 0;
+        }
+    }
+    c1 = tc1;
+    for (int i = 2; i < numVerts; i++) {
+        float4 c2 = lerpClip(ov0, od1, od2, bary[i * 2], bary[i * 2 + 1]);
+        SnapOut sn = snapTriangle(c0, c1, c2, width, height);
+        if (prepareTriangle<S>(sn, width, height, d1, d2, area) == 0) {
+            setupTriangle<S, F>(&d.triHeader[base], &d.triData[base * 4], vidx, c0, c1, c2,
+                                make_float2(bary[0], bary[1]), make_float2(bary[i * 2 - 2], bary[i * 2 - 1]),
+                                make_float2(bary[i * 2], bary[i * 2 + 1]), sn, d1, d2, area, width, height);
+            base++;
+        }
+        c1 = c2;
+    }
+}
+
 // triangleSetupImpl (TriangleSetup.inl:219-417), over the triangle range of
 // one pipe group [triBegin, triEnd) (global triangle slots).
 template <int S, U32 F>
-__global__ void __launch_bounds__(256) setupKernel(DrawDev d, int instBegin, int instEnd, S64 triBegin, S64 triEnd) {
+__global__ void __launch_bounds__(256, 4) setupKernel(DrawDev d, int instBegin, int instEnd, S64 triBegin, S64 triEnd) {
     S64 gt = triBegin + (S64)blockIdx.x * 256 + threadIdx.x;
     if (gt >= triEnd) return;
     int ii = instBegin + findInstance64(d.triPrefix + instBegin, instEnd - instBegin, gt);
@@ -174,46 +222,8 @@ __global__ void __launch_bounds__(256) setupKernel(DrawDev d, int instBegin, int
         }
     }
 
-    // Clip to the view frustum (TriangleSetup.inl:326-412).
-    float4 ov0 = v0;
-    float4 od1 = make_float4(fsub(v1.x, v0.x), fsub(v1.y, v0.y), fsub(v1.z, v0.z), fsub(v1.w, v0.w));
-    float4 od2 = make_float4(fsub(v2.x, v0.x), fsub(v2.y, v0.y), fsub(v2.z, v0.z), fsub(v2.w, v0.w));
-    F32 bary[18];
-    int numVerts = clipTriangle(bary, &ov0.x, &v1.x, &v2.x, &od1.x, &od2.x);
-    float4 c0 = lerpClip(ov0, od1, od2, bary[0], bary[1]);
-    float4 c1 = lerpClip(ov0, od1, od2, bary[2], bary[3]);
-    float4 tc1 = c1;
-
-    int numSubtris = 0;
-    for (int i = 2; i < numVerts; i++) {
-        float4 c2 = lerpClip(ov0, od1, od2, bary[i * 2], bary[i * 2 + 1]);
-        SnapOut sn = snapTriangle(c0, c1, c2, width, height);
-        if (prepareTriangle<S>(sn, width, height, d1, d2, area) == 0) numSubtris++;
-        c1 = c2;
-    }
-    d.triSubtris[gt] = (uint8_t)numSubtris;
-
-    S64 base = gt;
-    if (numSubtris > 1) {
-        base = d.totalTris + atomicAdd(&d.counters->extraSubtris, numSubtris);
-        d.triHeader[gt].w = (U32)base;
-        if (base + numSubtris > d.maxSubtris) {
-            atomicOr(&d.counters->overflow, kOverflowSubtris);
-            numVerts = 0;
-        }
-    }
-    c1 = tc1;
-    for (int i = 2; i < numVerts; i++) {
-        float4 c2 = lerpClip(ov0, od1, od2, bary[i * 2], bary[i * 2 + 1]);
-        SnapOut sn = snapTriangle(c0, c1, c2, width, height);
-        if (prepareTriangle<S>(sn, width, height, d1, d2, area) == 0) {
-            setupTriangle<S, F>(&d.triHeader[base], &d.triData[base * 4], vidx, c0, c1, c2,
-                                make_float2(bary[0], bary[1]), make_float2(bary[i * 2 - 2], bary[i * 2 - 1]),
-                                make_float2(bary[i * 2], bary[i * 2 + 1]), sn, d1, d2, area, width, height);
-            base++;
-        }
-        c1 = c2;
-    }
+    // Clip to the view frustum (TriangleSetup.inl:326-412); rare, kept out of line.
+    setupClipped<S, F>(d, gt, vidx, v0, v1, v2, width, height);
 }
 
 }  // namespace cr
