@@ -78,6 +78,14 @@ _SIGNATURES = {
     "cr_draw_triangles_async": (C.c_int, [C.c_void_p, C.c_void_p]),
     "cr_draw_batch": (C.c_int, [C.c_void_p, C.POINTER(Instance), C.c_int32, C.c_void_p]),
     "cr_draw_batch_async": (C.c_int, [C.c_void_p, C.POINTER(Instance), C.c_int32, C.c_void_p]),
+    "cr_batch_graph_create": (C.c_int, [C.c_void_p, C.POINTER(Instance), C.c_int32, C.c_void_p,
+                                        C.POINTER(C.c_void_p)]),
+    "cr_batch_graph_launch": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "cr_batch_graph_counters": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(Counters)]),
+    "cr_batch_graph_destroy": (C.c_int, [C.c_void_p]),
+    "cr_draw_triangles_static": (C.c_int, [C.c_char_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
+                                           C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_uint32, C.c_uint32,
+                                           C.c_void_p, C.c_char_p, C.c_int64]),
     "cr_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     "cr_get_counters": (C.c_int, [C.c_void_p, C.POINTER(Counters)]),
     "cr_get_profiling_info": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),

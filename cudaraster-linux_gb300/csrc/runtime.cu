@@ -104,6 +104,7 @@ struct cr_context {
     cr_tuning tuning{};
     // Capacities (elements), grown by the rerun loop and kept across draws.
     int64_t maxSubtris = 0, maxBinEntries = 0, maxTileEntries = 0;
+    bool userCapacity = false;  // capacities set by cr_set_capacity replace the estimates
     // Device memory.
     DevBuf triSubtris, triHeader, triData, chunkBinCount, binCount, binStart, binUnitFirst, binList;
     DevBuf unitBin, unitSeg, unitTileCount, tileCount, tileStart, tileList, instBuf, prefixBuf, counters, fineCounters;
@@ -360,6 +361,7 @@ cr_status cr_set_capacity(cr_context* ctx, int64_t ms, int64_t mb, int64_t mt) {
     ctx->maxSubtris = ms;
     ctx->maxBinEntries = mb;
     ctx->maxTileEntries = mt;
+    ctx->userCapacity = (ms | mb | mt) != 0;
     return CR_OK;
 }
 
@@ -461,9 +463,17 @@ cr_status ensureCapacity(cr_context* ctx, const Plan& plan) {
     int64_t T = plan.totalTris;
     // Initial sizes in the spirit of CudaRaster.cpp:263-275 (subtriangle
     // slack 4096; queues scaled with the triangle count), grown on overflow.
-    ctx->maxSubtris = std::max<int64_t>(ctx->maxSubtris, T + 4096);
-    ctx->maxBinEntries = std::max<int64_t>(ctx->maxBinEntries, 2 * T + 65536);
-    ctx->maxTileEntries = std::max<int64_t>(ctx->maxTileEntries, 4 * T + 65536);
+    if (ctx->userCapacity) {
+        // Capacities chosen by the caller (e.g. a predictor): only the
+        // triangle slots themselves are guaranteed.
+        ctx->maxSubtris = std::max<int64_t>(ctx->maxSubtris, T);
+        ctx->maxBinEntries = std::max<int64_t>(ctx->maxBinEntries, 1);
+        ctx->maxTileEntries = std::max<int64_t>(ctx->maxTileEntries, 1);
+    } else {
+        ctx->maxSubtris = std::max<int64_t>(ctx->maxSubtris, T + 4096);
+        ctx->maxBinEntries = std::max<int64_t>(ctx->maxBinEntries, 2 * T + 65536);
+        ctx->maxTileEntries = std::max<int64_t>(ctx->maxTileEntries, 4 * T + 65536);
+    }
     const int tpb = 1 << (2 * plan.binLog2);
     int64_t maxUnits = ctx->maxBinEntries / plan.unitEntries + plan.totalBins + 1;
     CR_CUDA(ctx->triSubtris.ensure((size_t)std::max<int64_t>(T, 1)), "cudaMalloc");
@@ -536,12 +546,17 @@ DrawDev makeDrawDev(cr_context* ctx, const Plan& plan) {
     return d;
 }
 
-cr_status launchDraw(cr_context* ctx, const Plan& plan, cudaStream_t stream) {
+// Enqueues one draw of `plan` on `stream`. `stage` is pinned host memory for
+// the descriptors (the copy node reads it when a captured graph replays) and
+// `hostCounters` receives the device counters; with `events` false no stage
+// events are recorded (graph capture).
+cr_status launchDrawWith(cr_context* ctx, const Plan& plan, cudaStream_t stream, void* stage, Counters* hostCounters,
+                         bool events) {
     DrawDev d = makeDrawDev(ctx, plan);
     // Stage the descriptors through pinned memory.
     size_t n1 = plan.inst.size() + 1;
     size_t instBytes = sizeof(InstanceDev) * plan.inst.size();
-    char* hs = (char*)ctx->hostStage;
+    char* hs = (char*)stage;
     for (size_t i = 0; i < plan.inst.size(); i++) memcpy(hs + i * sizeof(InstanceDev), &plan.inst[i].dev, sizeof(InstanceDev));
     char* hp = hs + instBytes;
     memcpy(hp, plan.triPrefix.data(), 8 * n1);
@@ -553,23 +568,29 @@ cr_status launchDraw(cr_context* ctx, const Plan& plan, cudaStream_t stream) {
     CR_CUDA(cudaMemsetAsync(ctx->counters.ptr, 0, sizeof(Counters), stream), "cudaMemsetAsync");
     CR_CUDA(cudaMemsetAsync(ctx->fineCounters.ptr, 0, sizeof(int32_t) * plan.groups.size(), stream), "cudaMemsetAsync");
 
-    CR_CUDA(cudaEventRecord(ctx->ev[0], stream), "cudaEventRecord");
+    if (events) CR_CUDA(cudaEventRecord(ctx->ev[0], stream), "cudaEventRecord");
     for (const Plan::Group& g : plan.groups)
         CR_CUDA(g.pipe->launchSetup(d, g.instBegin, g.instEnd, g.triBegin, g.triEnd, stream), "setup launch");
-    CR_CUDA(cudaEventRecord(ctx->ev[1], stream), "cudaEventRecord");
-    CR_CUDA(launchBinning(d, plan.maxBins, ctx->numSMs, stream, ctx->ev[2]), "bin/coarse launch");
-    CR_CUDA(cudaEventRecord(ctx->ev[3], stream), "cudaEventRecord");
+    if (events) CR_CUDA(cudaEventRecord(ctx->ev[1], stream), "cudaEventRecord");
+    CR_CUDA(launchBinning(d, plan.maxBins, ctx->numSMs, stream, events ? ctx->ev[2] : nullptr), "bin/coarse launch");
+    if (events) CR_CUDA(cudaEventRecord(ctx->ev[3], stream), "cudaEventRecord");
     int warps = ctx->tuning.fine_warps > 0 ? ctx->tuning.fine_warps : 8;
     for (size_t gi = 0; gi < plan.groups.size(); gi++) {
         const Plan::Group& g = plan.groups[gi];
         int ctas = ctx->tuning.fine_ctas_per_sm > 0 ? ctx->tuning.fine_ctas_per_sm : g.pipe->fineOccupancy(warps);
         CR_CUDA(g.pipe->launchFine(d, (int)gi, g.tileBegin, g.tileEnd, warps, ctas, ctx->numSMs, stream), "fine launch");
     }
-    CR_CUDA(cudaEventRecord(ctx->ev[4], stream), "cudaEventRecord");
-    ctx->eventsRecorded = true;
-    CR_CUDA(cudaMemcpyAsync(ctx->hostCounters, ctx->counters.ptr, sizeof(Counters), cudaMemcpyDeviceToHost, stream),
+    if (events) {
+        CR_CUDA(cudaEventRecord(ctx->ev[4], stream), "cudaEventRecord");
+        ctx->eventsRecorded = true;
+    }
+    CR_CUDA(cudaMemcpyAsync(hostCounters, ctx->counters.ptr, sizeof(Counters), cudaMemcpyDeviceToHost, stream),
             "cudaMemcpyAsync");
     return CR_OK;
+}
+
+cr_status launchDraw(cr_context* ctx, const Plan& plan, cudaStream_t stream) {
+    return launchDrawWith(ctx, plan, stream, ctx->hostStage, ctx->hostCounters, true);
 }
 
 void recordCounters(cr_context* ctx, const Plan& plan, int reruns) {
@@ -647,9 +668,8 @@ cr_status drawCurrent(cr_context* ctx, void* stream, bool sync) {
     return st;
 }
 
-cr_status drawBatch(cr_context* ctx, const cr_instance* instances, int32_t count, void* stream, bool sync) {
+cr_status batchInstances(cr_context* ctx, const cr_instance* instances, int32_t count, std::vector<HostInstance>& v) {
     if (!ctx || (!instances && count > 0) || count < 0) return CR_ERR_INVALID_ARGUMENT;
-    std::vector<HostInstance> v;
     for (int i = 0; i < count; i++) {
         const cr_instance& s = instances[i];
         const PipeDesc* p = s.pipe ? findPipe(s.pipe) : nullptr;
@@ -682,18 +702,120 @@ cr_status drawBatch(cr_context* ctx, const cr_instance* instances, int32_t count
         h.dev.clearDepth = s.clear_depth;
         v.push_back(h);
     }
-    if (v.empty()) return CR_OK;
+    return CR_OK;
+}
+
+cr_status drawBatch(cr_context* ctx, const cr_instance* instances, int32_t count, void* stream, bool sync) {
+    std::vector<HostInstance> v;
+    cr_status st = batchInstances(ctx, instances, count, v);
+    if (st != CR_OK || v.empty()) return st;
     Plan plan;
-    cr_status st = buildPlan(ctx, v, plan);
+    st = buildPlan(ctx, v, plan);
     if (st != CR_OK) return st;
     return drawPlan(ctx, plan, (cudaStream_t)stream, sync);
 }
 
 }  // namespace
 
+// A batched draw captured once into a CUDA graph and replayed per frame
+// (descriptor copies, counter resets, every kernel and the counter read-back
+// are graph nodes). Overflow cannot rerun inside a graph: the kernels skip the
+// frame and raise a flag, and cr_batch_graph_counters reports it so the host
+// grows the queues and recaptures.
+struct cr_batch_graph {
+    cr_context* ctx = nullptr;
+    Plan plan;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    void* stage = nullptr;
+    Counters* counters = nullptr;
+};
+
 extern "C" {
 
 cr_status cr_draw_triangles(cr_context* ctx, void* stream) { return drawCurrent(ctx, stream, true); }
+
+cr_status cr_batch_graph_create(cr_context* ctx, const cr_instance* instances, int32_t count, void* stream,
+                                cr_batch_graph** out) {
+    if (!ctx || !out) return CR_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    std::vector<HostInstance> v;
+    cr_status st = batchInstances(ctx, instances, count, v);
+    if (st != CR_OK) return st;
+    if (v.empty()) return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaRaster: empty batch");
+    cr_batch_graph* g = new cr_batch_graph();
+    g->ctx = ctx;
+    st = buildPlan(ctx, v, g->plan);
+    if (st == CR_OK) st = ensureCapacity(ctx, g->plan);
+    if (st != CR_OK) { delete g; return st; }
+    size_t stageBytes = sizeof(InstanceDev) * g->plan.inst.size() + 20 * (g->plan.inst.size() + 1) + 64;
+    cudaError_t e = cudaMallocHost(&g->stage, stageBytes);
+    if (e == cudaSuccess) e = cudaMallocHost(&g->counters, sizeof(Counters));
+    if (e != cudaSuccess) {
+        if (g->stage) cudaFreeHost(g->stage);
+        delete g;
+        return cudaFail(ctx, e, "cudaMallocHost");
+    }
+    memset(g->counters, 0, sizeof(Counters));
+    // Capture on a private stream ordered after `stream`.
+    cudaStream_t cap;
+    e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { cr_batch_graph_destroy(g); return cudaFail(ctx, e, "cudaStreamCreate"); }
+    cudaStreamSynchronize((cudaStream_t)stream);
+    e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        st = launchDrawWith(ctx, g->plan, cap, g->stage, g->counters, false);
+        cudaError_t e2 = cudaStreamEndCapture(cap, &g->graph);
+        if (st == CR_OK && e2 != cudaSuccess) st = cudaFail(ctx, e2, "cudaStreamEndCapture");
+    } else {
+        st = cudaFail(ctx, e, "cudaStreamBeginCapture");
+    }
+    cudaStreamDestroy(cap);
+    if (st == CR_OK) {
+        e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+        if (e != cudaSuccess) st = cudaFail(ctx, e, "cudaGraphInstantiate");
+    }
+    if (st != CR_OK) { cr_batch_graph_destroy(g); return st; }
+    *out = g;
+    return CR_OK;
+}
+
+cr_status cr_batch_graph_launch(cr_batch_graph* g, void* stream) {
+    if (!g) return CR_ERR_INVALID_ARGUMENT;
+    cudaError_t e = cudaGraphLaunch(g->exec, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cudaFail(g->ctx, e, "cudaGraphLaunch");
+    return CR_OK;
+}
+
+cr_status cr_batch_graph_counters(cr_batch_graph* g, void* stream, cr_counters* out) {
+    if (!g || !out) return CR_ERR_INVALID_ARGUMENT;
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return cudaFail(g->ctx, e, "cudaStreamSynchronize");
+    const Counters& c = *g->counters;
+    memset(out, 0, sizeof(*out));
+    out->num_tris = g->plan.totalTris;
+    out->num_subtris = g->plan.totalTris + c.extraSubtris;
+    out->bin_entries = c.binEntries;
+    out->tile_entries = c.tileEntries;
+    out->coarse_units = c.numUnits;
+    out->max_subtris = g->ctx->maxSubtris;
+    out->max_bin_entries = g->ctx->maxBinEntries;
+    out->max_tile_entries = g->ctx->maxTileEntries;
+    out->overflow = c.overflow;
+    out->num_bins = g->plan.totalBins;
+    out->num_tiles = g->plan.totalTiles;
+    return CR_OK;
+}
+
+cr_status cr_batch_graph_destroy(cr_batch_graph* g) {
+    if (!g) return CR_ERR_INVALID_ARGUMENT;
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    if (g->stage) cudaFreeHost(g->stage);
+    if (g->counters) cudaFreeHost(g->counters);
+    delete g;
+    return CR_OK;
+}
 cr_status cr_draw_triangles_async(cr_context* ctx, void* stream) { return drawCurrent(ctx, stream, false); }
 cr_status cr_draw_batch(cr_context* ctx, const cr_instance* inst, int32_t n, void* stream) {
     return drawBatch(ctx, inst, n, stream, true);

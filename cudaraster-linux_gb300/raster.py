@@ -234,11 +234,7 @@ class CudaRaster:
         s = (stream or torch.cuda.current_stream()).cuda_stream
         self._check(self._lib.cr_draw_triangles_async(self._ctx, C.c_void_p(s)))
 
-    def drawBatch(self, instances: list[dict], stream: torch.cuda.Stream | None = None, sync: bool = True) -> None:
-        """Draw several independent scenes in one set of launches. Each dict has
-        pipe, color, depth (CudaSurface), vertices, indices (tensor/Buffer),
-        numTris and optionally clear=(r, g, b, a, depth)."""
-        self._need_init()
+    def _instances(self, instances: list[dict]):
         arr = (_lib.Instance * len(instances))()
         keep = []
         for i, d in enumerate(instances):
@@ -258,9 +254,26 @@ class CudaRaster:
                 arr[i].deferred_clear = 1
                 arr[i].clear_color = self._lib.cr_color_to_abgr(*[float(c) for c in clear[:4]])
                 arr[i].clear_depth = self._lib.cr_clear_depth_from_float(float(clear[4]))
+        return arr, keep
+
+    def drawBatch(self, instances: list[dict], stream: torch.cuda.Stream | None = None, sync: bool = True) -> None:
+        """Draw several independent scenes in one set of launches. Each dict has
+        pipe, color, depth (CudaSurface), vertices, indices (tensor/Buffer),
+        numTris and optionally clear=(r, g, b, a, depth)."""
+        self._need_init()
+        arr, keep = self._instances(instances)
         s = (stream or torch.cuda.current_stream()).cuda_stream
         fn = self._lib.cr_draw_batch if sync else self._lib.cr_draw_batch_async
         self._check(fn(self._ctx, arr, len(instances), C.c_void_p(s)))
+
+    def createBatchGraph(self, instances: list[dict], stream: torch.cuda.Stream | None = None) -> "BatchGraph":
+        """Capture the batched draw of `instances` into a CUDA graph (see cr_batch_graph_create)."""
+        self._need_init()
+        arr, keep = self._instances(instances)
+        s = (stream or torch.cuda.current_stream()).cuda_stream
+        h = C.c_void_p()
+        self._check(self._lib.cr_batch_graph_create(self._ctx, arr, len(instances), C.c_void_p(s), C.byref(h)))
+        return BatchGraph(self, h, keep, instances)
 
     def getStats(self) -> Stats:
         self._need_init()
@@ -285,6 +298,36 @@ class CudaRaster:
         d = _lib.DebugParams(int(p.emulateTriangleSetup), int(p.emulateBinRaster), int(p.emulateCoarseRaster),
                              int(p.emulateFineRaster))
         self._check(self._lib.cr_set_debug_params(self._ctx, C.byref(d)))
+
+
+class BatchGraph:
+    """A captured batched draw; launch() replays it asynchronously."""
+
+    def __init__(self, raster: CudaRaster, handle, keep, instances):
+        self._raster = raster
+        self._h = handle
+        self._keep = (keep, instances)
+
+    def launch(self, stream: torch.cuda.Stream | None = None) -> None:
+        s = (stream or torch.cuda.current_stream()).cuda_stream
+        self._raster._check(self._raster._lib.cr_batch_graph_launch(self._h, C.c_void_p(s)))
+
+    def counters(self, stream: torch.cuda.Stream | None = None) -> dict:
+        s = (stream or torch.cuda.current_stream()).cuda_stream
+        c = _lib.Counters()
+        self._raster._check(self._raster._lib.cr_batch_graph_counters(self._h, C.c_void_p(s), C.byref(c)))
+        return {f: getattr(c, f) for f, _ in _lib.Counters._fields_}
+
+    def destroy(self) -> None:
+        if self._h:
+            self._raster._lib.cr_batch_graph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
 
 
 def _ptr_of(buf) -> int | None:

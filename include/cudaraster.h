@@ -154,8 +154,10 @@ cr_status cr_set_index_buffer(cr_context* ctx, const void* indices, int64_t offs
                               int32_t num_tris);
 cr_status cr_set_tuning(cr_context* ctx, const cr_tuning* tuning);
 cr_status cr_set_debug_params(cr_context* ctx, const cr_debug_params* params);
-/* Initial capacities (elements). Zero keeps the reference's estimates
- * (CudaRaster.cpp:263-275); undersized values are grown by the rerun loop. */
+/* Queue capacities (elements) for the next draws. All zero keeps the
+ * reference-style estimates (CudaRaster.cpp:263-275); otherwise the given
+ * sizes are used as they are (a predictor's sizing) and, when a draw
+ * overflows them, grown by the rerun loop. Capacities never shrink. */
 cr_status cr_set_capacity(cr_context* ctx, int64_t max_subtris, int64_t max_bin_entries,
                           int64_t max_tile_entries);
 
@@ -171,6 +173,20 @@ cr_status cr_draw_triangles_async(cr_context* ctx, void* stream);
 /* Several independent scenes in one set of launches. */
 cr_status cr_draw_batch(cr_context* ctx, const cr_instance* instances, int32_t count, void* stream);
 cr_status cr_draw_batch_async(cr_context* ctx, const cr_instance* instances, int32_t count, void* stream);
+
+/* Batched draw captured into a CUDA graph (no counterpart in the reference).
+ * Capture fixes the batch (surfaces, buffers, triangle counts, pipes) and the
+ * queue capacities of `ctx` at that moment; replays are asynchronous. A
+ * replay whose queues overflow skips the frame (surfaces untouched) and sets
+ * `overflow` in cr_batch_graph_counters: grow the capacities
+ * (cr_set_capacity) and recapture. While a graph is alive, other draws on the
+ * same context must not need larger queues (they would reallocate them). */
+typedef struct cr_batch_graph cr_batch_graph;
+cr_status cr_batch_graph_create(cr_context* ctx, const cr_instance* instances, int32_t count, void* stream,
+                                cr_batch_graph** out);
+cr_status cr_batch_graph_launch(cr_batch_graph* graph, void* stream);
+cr_status cr_batch_graph_counters(cr_batch_graph* graph, void* stream, cr_counters* out);
+cr_status cr_batch_graph_destroy(cr_batch_graph* graph);
 
 /* No counterpart in the reference. The same draw as cr_draw_triangles for
  * callers that may not allocate memory while they run (a host application
