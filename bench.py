@@ -151,6 +151,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the uneven-batch comparison")
     ap.add_argument("--profile-frames", type=int, default=0,
                     help="only draw this many frames of the workload (for ncu captures), print nothing else")
     args = ap.parse_args()
@@ -170,8 +171,12 @@ def main():
     T = sc["indices"].shape[0]
     W, H = sc["width"], sc["height"]
 
+    workloads = importlib.import_module(PKG + ".workloads")
+    tuning = workloads.load_tuning("soup1m")
     cr = pkg.CudaRaster()
     cr.init()
+    if tuning:
+        cr.setTuning(**tuning)
     color = pkg.CudaSurface((W, H), pkg.CudaSurface.FORMAT_RGBA8, 1)
     depth = pkg.CudaSurface((W, H), pkg.CudaSurface.FORMAT_DEPTH32, 1)
     cr.setSurfaces(color, depth)
@@ -299,7 +304,14 @@ def main():
             "e2e": {"value": round(e2e_value, 3), "unit": "frames/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_total / args.steps, 4)},
             "roofline": roofline, "clocks": clk.summary(),
-            "gpu_launches": 8 * args.steps, "counters": counters}
+            "gpu_launches": 8 * args.steps, "counters": counters, "tuning": tuning}
+    if not args.no_batch:
+        scenes = importlib.import_module(PKG + ".scenes")
+        batch = workloads.Batch(scenes.batch(64, seed=4))
+        line["batched"] = dict(workloads.measure_batch(batch, steps=5, tuning=workloads.load_tuning("batch64")),
+                               workload="uneven batch: 64 random soups, 1k-500k triangles (log-uniform), "
+                                        "resolutions 256^2..1920x1080, half src-over blended; "
+                                        "plain = 64 sequential drawTriangles, batched = one CUDA-graph replay")
     if rank == 0 and not args.no_cpu_baseline:
         cb, (rc, rd, st) = cpu_baseline(sc)
         gc = color.download().numpy().astype(np.uint32)
