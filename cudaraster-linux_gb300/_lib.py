@@ -86,6 +86,8 @@ _SIGNATURES = {
     "cr_draw_triangles_static": (C.c_int, [C.c_char_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
                                            C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_uint32, C.c_uint32,
                                            C.c_void_p, C.c_char_p, C.c_int64]),
+    "cr_vertex_shader_passthrough": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
+                                               C.c_int64, C.POINTER(C.c_float), C.c_void_p]),
     "cr_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     "cr_get_counters": (C.c_int, [C.c_void_p, C.POINTER(Counters)]),
     "cr_get_profiling_info": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),

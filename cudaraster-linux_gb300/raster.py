@@ -342,6 +342,37 @@ def _ptr_of(buf) -> int | None:
     return int(buf)
 
 
+def vertex_shader_passthrough(model: torch.Tensor, mvp, colors: torch.Tensor | None = None,
+                              out: torch.Tensor | None = None, stream: torch.cuda.Stream | None = None) -> torch.Tensor:
+    """clip = MVP * (model, 1) on the GPU (the reference's vertexShader_passthrough).
+    model: [N, >=3] float32 CUDA tensor; colors: optional [N, 4]; returns [N, 8] (or [N, 4]) records."""
+    lib = _lib.load()
+    n = model.shape[0]
+    width = 8 if colors is not None else 4
+    if out is None:
+        out = torch.empty((n, width), dtype=torch.float32, device=model.device)
+    m = (C.c_float * 16)(*[float(x) for x in torch.as_tensor(mvp, dtype=torch.float32).reshape(-1).tolist()])
+    s = (stream or torch.cuda.current_stream()).cuda_stream
+    check(lib.cr_vertex_shader_passthrough(model.data_ptr(), model.stride(0), colors.data_ptr() if colors is not None
+                                           else None, colors.stride(0) if colors is not None else 0, out.data_ptr(),
+                                           width * 4, n, m, C.c_void_p(s)))
+    return out
+
+
+def vertex_shader_reference(model, mvp):
+    """Host restatement (numpy float32) of the same product, used by tests."""
+    import numpy as np
+    m = np.asarray(mvp, dtype=np.float32).reshape(4, 4)
+    v = np.asarray(model, dtype=np.float32)
+    out = np.empty((v.shape[0], 4), np.float32)
+    for r in range(4):
+        acc = np.zeros(v.shape[0], np.float32)
+        for c in range(3):
+            acc = acc + m[r, c] * v[:, c]
+        out[:, r] = acc + m[r, 3] * np.float32(1.0)
+    return out
+
+
 def encode_depth(d: int) -> int:
     return _lib.load().cr_encode_depth(d)
 

@@ -206,6 +206,17 @@ cr_status cr_draw_triangles_static(const char* pipe, void* color, void* depth, i
                                    int32_t num_tris, int32_t deferred_clear, uint32_t clear_color,
                                    uint32_t clear_depth, void* stream, char* error, int64_t error_size);
 
+/* ---- Vertex stage ---- */
+/* The reference's vertexShader_passthrough (test/shader/PassThrough.cu:16-35):
+ * out[i].clipPos = MVP * (model[i].xyz, 1), Mat4f * Vec4f accumulated in the
+ * framework's order (Math.hpp:990-1001). model: float triplets at
+ * model_stride floats; colors (optional, may be NULL): RGBA floats at
+ * color_stride copied behind the position; out: 16- or 32-byte records
+ * (ShadedVertexBase / GouraudVertex). Device pointers; asynchronous. */
+cr_status cr_vertex_shader_passthrough(const float* model, int32_t model_stride, const float* colors,
+                                       int32_t color_stride, void* out_vertices, int32_t out_stride_bytes,
+                                       int64_t num_vertices, const float* mvp_row_major, void* stream);
+
 /* ---- Results ---- */
 cr_status cr_get_stats(cr_context* ctx, cr_stats* out);
 cr_status cr_get_counters(cr_context* ctx, cr_counters* out);
