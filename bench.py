@@ -53,6 +53,15 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def stage_traffic(stage: str):
+    """DRAM bytes (read + write) of one launch of a stage's kernels on this
+    workload, from the committed ncu summary of the same command, or None."""
+    p = ROOT / "profiles" / "stages_soup1m_1080p.traffic.json"
+    if not p.exists():
+        return None
+    return json.loads(p.read_text())["dram_bytes_per_stage"].get(stage)
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -276,22 +285,22 @@ def main():
     names = ["setup", "bin", "coarse", "fine"]
     dom = int(np.argmax(stage_ms))
     V = sc["vertices"].shape[0]
-    # Algorithmic bytes per launch of each stage (one frame):
-    #   setup : index 12 B + clipPos 16 B x 3 vertices read, subtri byte + header 16 B + data 64 B written per triangle
-    #   bin   : subtri count + header per triangle read twice (count, scatter), 4 B per bin entry written
-    #   coarse: 4 B entry + 16 B header per bin entry read twice, 4 B per tile entry written
-    #   fine  : per tile entry 4 B + header 16 B + data 64 B, colour+depth of every sample written once
+    # Algorithmic bytes per launch of each stage (one frame), each byte counted once:
+    #   setup : index 12 B per triangle, each clip position 16 B once; subtri byte + header 16 B + data 64 B written
+    #   bin   : subtri byte + header per triangle read, 4 B per bin entry written
+    #   coarse: 4 B entry + 16 B header per bin entry read, 4 B per tile entry written
+    #   fine  : 4 B per tile entry, header + data once per bin entry, colour + depth of every sample written
     N = ((W + 7) // 8 * 8) * ((H + 7) // 8 * 8)
     alg = {
-        "setup": T * (12 + 48 + 1 + 16 + 64),
-        "bin": T * 2 * (1 + 16) + counters["bin_entries"] * 4,
-        "coarse": counters["bin_entries"] * 2 * (4 + 16) + counters["tile_entries"] * 4,
-        "fine": counters["tile_entries"] * (4 + 16 + 64) + N * 8,
+        "setup": T * (12 + 1 + 16 + 64) + V * 16,
+        "bin": T * 17 + counters["bin_entries"] * 4,
+        "coarse": counters["bin_entries"] * 20 + counters["tile_entries"] * 4,
+        "fine": counters["tile_entries"] * 4 + counters["bin_entries"] * 80 + N * 8,
     }
     achieved = alg[names[dom]] / (stage_ms[dom] / 1e3) / 1e9
     roofline = {"bound": "hbm", "kernel": names[dom], "achieved": round(achieved, 1), "peak": peak,
                 "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                "traffic": None, "alg_bytes_per_launch": int(alg[names[dom]]),
+                "traffic": stage_traffic(names[dom]), "alg_bytes_per_launch": int(alg[names[dom]]),
                 "stage_ms": {n: round(float(m), 4) for n, m in zip(names, stage_ms)}}
     b_alg = 12 * T + 32 * V + 8 * N
     frame_frac = b_alg / (ms_per_step / 1e3) / 1e9 / peak
