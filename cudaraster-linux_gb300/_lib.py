@@ -58,6 +58,12 @@ class Instance(C.Structure):
                 ("clear_color", C.c_uint32), ("clear_depth", C.c_uint32)]
 
 
+class QueueLayout(C.Structure):
+    _fields_ = [("bins_x", C.c_int32), ("bins_y", C.c_int32), ("tiles_x", C.c_int32), ("tiles_y", C.c_int32),
+                ("bin_log2", C.c_int32), ("num_bins", C.c_int32), ("num_tiles", C.c_int32),
+                ("num_instances", C.c_int32)]
+
+
 # name -> (restype, argtypes)
 _SIGNATURES = {
     "cr_abi_version": (C.c_int32, []),
@@ -88,6 +94,33 @@ _SIGNATURES = {
                                            C.c_void_p, C.c_char_p, C.c_int64]),
     "cr_vertex_shader_passthrough": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
                                                C.c_int64, C.POINTER(C.c_float), C.c_void_p]),
+    "cr_get_queue_layout": (C.c_int, [C.c_void_p, C.POINTER(QueueLayout)]),
+    "cr_queue_counts": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
+    "cr_queue_features": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_float), C.c_void_p, C.c_void_p]),
+    "cr_queue_log_counts": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                      C.c_void_p, C.c_void_p]),
+    "cr_queue_targets": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p,
+                                   C.c_void_p]),
+    "cr_queue_plan": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
+                                C.c_void_p]),
+    "cr_predictor_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
+    "cr_predictor_destroy": (None, [C.c_void_p]),
+    "cr_predictor_num_params": (C.c_int64, [C.c_void_p]),
+    "cr_predictor_steps": (C.c_int64, [C.c_void_p]),
+    "cr_predictor_set_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int64]),
+    "cr_predictor_get_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int64]),
+    "cr_predictor_get_params_bf16": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint16), C.c_int64]),
+    "cr_predictor_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
+    "cr_predictor_gradients": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
+                                         C.c_void_p, C.c_void_p, C.c_void_p]),
+    "cr_predictor_train_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
+                                          C.c_float, C.c_float, C.c_float, C.c_float, C.c_void_p, C.c_void_p]),
+    "cr_predictor_bad_rows": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_int32]),
+    "cr_predictor_frame": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(QueueLayout),
+                                     C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.POINTER(C.c_float), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "cr_get_queue_buffers": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                       C.POINTER(C.c_void_p)]),
     "cr_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     "cr_get_counters": (C.c_int, [C.c_void_p, C.POINTER(Counters)]),
     "cr_get_profiling_info": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),

@@ -61,12 +61,16 @@ namespace {
 struct DevBuf {
     void* ptr = nullptr;
     size_t bytes = 0;
+    // Grows only. A regrow takes a quarter more than asked, so queues whose
+    // capacity creeps up from draw to draw (e.g. sized by a predictor) are
+    // not reallocated -- and the device synchronised -- every draw.
     cudaError_t ensure(size_t need) {
         if (need <= bytes) return cudaSuccess;
+        const bool regrow = ptr != nullptr;
         if (ptr) cudaFree(ptr);
         ptr = nullptr;
         bytes = 0;
-        size_t alloc = std::max<size_t>(need, 256);
+        size_t alloc = std::max<size_t>(regrow ? need + need / 4 : need, 256);
         cudaError_t e = cudaMalloc(&ptr, alloc);
         if (e == cudaSuccess) bytes = alloc;
         return e;
@@ -109,8 +113,15 @@ struct cr_context {
     DevBuf triSubtris, triHeader, triData, chunkBinCount, binCount, binStart, binUnitFirst, binList;
     DevBuf unitBin, unitSeg, unitTileCount, tileCount, tileStart, tileList, instBuf, prefixBuf, counters, fineCounters;
     // Pinned staging.
-    void* hostStage = nullptr;
-    size_t hostStageBytes = 0;
+    // Descriptor staging for asynchronous draws: a ring of pinned slots, each
+    // reused only after the copy that read it has run (stageDone), so a host
+    // that queues draw after draw never rewrites descriptors still in flight.
+    static constexpr int kStageSlots = 4;
+    void* hostStage[kStageSlots] = {};
+    size_t hostStageBytes = 0;                // per slot
+    cudaEvent_t stageDone[kStageSlots] = {};
+    bool stageUsed[kStageSlots] = {};
+    int stageNext = 0;
     Counters* hostCounters = nullptr;
     cudaEvent_t ev[5] = {};
     bool eventsRecorded = false;
@@ -118,6 +129,7 @@ struct cr_context {
     int device = 0;
     // Last draw.
     cr_counters last{};
+    cr_queue_layout lastLayout{};
 };
 
 namespace {
@@ -238,7 +250,10 @@ cr_status cr_destroy(cr_context* ctx) {
                       &ctx->unitTileCount, &ctx->tileCount, &ctx->tileStart, &ctx->tileList, &ctx->instBuf,
                       &ctx->prefixBuf, &ctx->counters, &ctx->fineCounters};
     for (DevBuf* b : bufs) b->release();
-    if (ctx->hostStage) cudaFreeHost(ctx->hostStage);
+    for (int i = 0; i < cr_context::kStageSlots; i++) {
+        if (ctx->hostStage[i]) cudaFreeHost(ctx->hostStage[i]);
+        if (ctx->stageDone[i]) cudaEventDestroy(ctx->stageDone[i]);
+    }
     if (ctx->hostCounters) cudaFreeHost(ctx->hostCounters);
     for (int i = 0; i < 5; i++)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
@@ -498,10 +513,18 @@ cr_status ensureCapacity(cr_context* ctx, const Plan& plan) {
     CR_CUDA(ctx->prefixBuf.ensure(prefBytes), "cudaMalloc");
     size_t stage = instBytes + prefBytes;
     if (stage > ctx->hostStageBytes) {
-        if (ctx->hostStage) cudaFreeHost(ctx->hostStage);
-        ctx->hostStage = nullptr;
+        for (int i = 0; i < cr_context::kStageSlots; i++) {
+            if (ctx->stageUsed[i]) CR_CUDA(cudaEventSynchronize(ctx->stageDone[i]), "cudaEventSynchronize");
+            ctx->stageUsed[i] = false;
+            if (ctx->hostStage[i]) cudaFreeHost(ctx->hostStage[i]);
+            ctx->hostStage[i] = nullptr;
+        }
         ctx->hostStageBytes = 0;
-        CR_CUDA(cudaMallocHost(&ctx->hostStage, stage * 2), "cudaMallocHost");
+        for (int i = 0; i < cr_context::kStageSlots; i++) {
+            CR_CUDA(cudaMallocHost(&ctx->hostStage[i], stage * 2), "cudaMallocHost");
+            if (!ctx->stageDone[i])
+                CR_CUDA(cudaEventCreateWithFlags(&ctx->stageDone[i], cudaEventDisableTiming), "cudaEventCreate");
+        }
         ctx->hostStageBytes = stage * 2;
     }
     return CR_OK;
@@ -590,7 +613,14 @@ cr_status launchDrawWith(cr_context* ctx, const Plan& plan, cudaStream_t stream,
 }
 
 cr_status launchDraw(cr_context* ctx, const Plan& plan, cudaStream_t stream) {
-    return launchDrawWith(ctx, plan, stream, ctx->hostStage, ctx->hostCounters, true);
+    const int slot = ctx->stageNext;
+    ctx->stageNext = (slot + 1) % cr_context::kStageSlots;
+    if (ctx->stageUsed[slot]) CR_CUDA(cudaEventSynchronize(ctx->stageDone[slot]), "cudaEventSynchronize");
+    cr_status st = launchDrawWith(ctx, plan, stream, ctx->hostStage[slot], ctx->hostCounters, true);
+    if (st != CR_OK) return st;
+    CR_CUDA(cudaEventRecord(ctx->stageDone[slot], stream), "cudaEventRecord");
+    ctx->stageUsed[slot] = true;
+    return CR_OK;
 }
 
 void recordCounters(cr_context* ctx, const Plan& plan, int reruns) {
@@ -613,6 +643,11 @@ void recordCounters(cr_context* ctx, const Plan& plan, int reruns) {
 cr_status drawPlan(cr_context* ctx, const Plan& plan, cudaStream_t stream, bool sync) {
     cr_status st = ensureCapacity(ctx, plan);
     if (st != CR_OK) return st;
+    const InstanceDev& first = plan.inst[0].dev;
+    ctx->lastLayout = cr_queue_layout{first.widthBins, first.heightBins, first.widthTiles, first.heightTiles,
+                                      plan.binLog2, plan.totalBins, plan.totalTiles, (int32_t)plan.inst.size()};
+    ctx->last.num_bins = plan.totalBins;
+    ctx->last.num_tiles = plan.totalTiles;
     for (int reruns = 0;; reruns++) {
         st = launchDraw(ctx, plan, stream);
         if (st != CR_OK) return st;
@@ -835,6 +870,43 @@ cr_status cr_get_stats(cr_context* ctx, cr_stats* out) {
     out->bin_time = t[1] * 1e-3f;
     out->coarse_time = t[2] * 1e-3f;
     out->fine_time = t[3] * 1e-3f;
+    return CR_OK;
+}
+
+cr_status cr_get_queue_layout(cr_context* ctx, cr_queue_layout* out) {
+    if (!ctx || !out) return CR_ERR_INVALID_ARGUMENT;
+    *out = ctx->lastLayout;
+    return CR_OK;
+}
+
+cr_status cr_get_queue_buffers(cr_context* ctx, const int32_t** bin_counts, const int32_t** tile_counts,
+                               const int32_t** counters) {
+    if (!ctx || !bin_counts || !tile_counts || !counters) return CR_ERR_INVALID_ARGUMENT;
+    if (ctx->lastLayout.num_bins == 0) return fail(ctx, CR_ERR_INVALID_STATE, "CudaRaster: no draw to take queue counts from");
+    *bin_counts = ctx->binCount.as<int32_t>();
+    *tile_counts = ctx->tileCount.as<int32_t>();
+    *counters = ctx->counters.as<int32_t>();
+    return CR_OK;
+}
+
+cr_status cr_queue_counts(cr_context* ctx, int32_t* bin_counts, int32_t num_bins, int32_t* tile_counts,
+                          int32_t num_tiles, int32_t* counters, void* stream) {
+    if (!ctx) return CR_ERR_INVALID_ARGUMENT;
+    const cr_queue_layout& l = ctx->lastLayout;
+    if (l.num_bins == 0) return fail(ctx, CR_ERR_INVALID_STATE, "CudaRaster: no draw to take queue counts from");
+    if ((bin_counts && num_bins != l.num_bins) || (tile_counts && num_tiles != l.num_tiles))
+        return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaRaster: queue count sizes %d/%d, last draw has %d bins, %d tiles",
+                    num_bins, num_tiles, l.num_bins, l.num_tiles);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (bin_counts)
+        CR_CUDA(cudaMemcpyAsync(bin_counts, ctx->binCount.ptr, (size_t)num_bins * 4, cudaMemcpyDeviceToDevice, s),
+                "cudaMemcpyAsync");
+    if (tile_counts)
+        CR_CUDA(cudaMemcpyAsync(tile_counts, ctx->tileCount.ptr, (size_t)num_tiles * 4, cudaMemcpyDeviceToDevice, s),
+                "cudaMemcpyAsync");
+    if (counters)
+        CR_CUDA(cudaMemcpyAsync(counters, ctx->counters.ptr, sizeof(Counters), cudaMemcpyDeviceToDevice, s),
+                "cudaMemcpyAsync");
     return CR_OK;
 }
 

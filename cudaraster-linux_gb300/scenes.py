@@ -157,16 +157,50 @@ def grid_mesh(n: int, seed: int = 0, amplitude: float = 0.2):
     return pos, rgba, tris
 
 
-def terrain_camera(frame: float = 0.0, width: int = 3840, height: int = 2160, elevation_deg: float = 15.0):
-    """Camera at a grazing angle above the heightfield; `frame` moves it along a closed spline."""
+def terrain_eye_target(frame: float = 0.0, elevation_deg: float = 15.0):
+    """Eye and target of the fly-through camera: a closed loop of 300 frames
+    around the heightfield, looking across it at a grazing angle."""
     t = frame * 2.0 * math.pi / 300.0
     ex = 1.25 * math.sin(t)
     ez = 1.25 * math.cos(t)
     dist = math.hypot(ex, ez)
     ey = 0.25 + dist * math.tan(math.radians(elevation_deg)) * 0.5
     target = (0.3 * math.sin(t + 0.7), 0.0, 0.3 * math.cos(t + 0.7))
-    mvp = perspective(60.0, width / height, 0.05, 10.0) @ look_at((ex, ey, ez), target)
-    return mvp
+    return np.array([ex, ey, ez]), np.array(target)
+
+
+def terrain_camera(frame: float = 0.0, width: int = 3840, height: int = 2160, elevation_deg: float = 15.0):
+    """Camera at a grazing angle above the heightfield; `frame` moves it along a closed spline."""
+    eye, target = terrain_eye_target(frame, elevation_deg)
+    return perspective(60.0, width / height, 0.05, 10.0) @ look_at(eye, target)
+
+
+def camera_delta(frame_a: float, frame_b: float, scale: float = 40.0) -> np.ndarray:
+    """6 floats describing the camera move from frame_a to frame_b: the eye's
+    displacement and the change of the unit view direction, both x scale."""
+    ea, ta = terrain_eye_target(frame_a)
+    eb, tb = terrain_eye_target(frame_b)
+    fa = (ta - ea) / np.linalg.norm(ta - ea)
+    fb = (tb - eb) / np.linalg.norm(tb - eb)
+    return (np.concatenate([eb - ea, fb - fa]) * scale).astype(np.float32)
+
+
+def water_mesh(n: int, level: float = -0.02, alpha: float = 0.35):
+    """Flat translucent n x n grid over [-1, 1]^2 at height `level` (the
+    fly-through's alpha-blended overlay layer)."""
+    xs = np.linspace(-1.0, 1.0, n)
+    X, Z = np.meshgrid(xs, xs)
+    pos = np.stack([X, np.full_like(X, level), Z], axis=-1).reshape(-1, 3)
+    ripple = 0.5 + 0.5 * np.sin(X * 37.0) * np.cos(Z * 29.0)
+    rgba = np.stack([0.1 + 0.1 * ripple, 0.3 + 0.2 * ripple, 0.6 + 0.2 * ripple, np.full_like(X, alpha)], axis=-1)
+    rgba = (np.round(rgba.reshape(-1, 4) * 255.0) / 255.0).astype(np.float32)
+    i = np.arange(n - 1)
+    I, J = np.meshgrid(i, i)
+    v00 = (J * n + I).reshape(-1)
+    tris = np.empty((2 * v00.size, 3), dtype=np.int32)
+    tris[0::2] = np.stack([v00, v00 + n, v00 + 1], axis=-1)
+    tris[1::2] = np.stack([v00 + 1, v00 + n, v00 + n + 1], axis=-1)
+    return pos, rgba, tris
 
 
 def terrain(n: int, width: int, height: int, samples: int = 1, seed: int = 0, frame: float = 0.0) -> dict:

@@ -107,3 +107,274 @@ def measure_batch(batch: Batch, steps: int = 5, warmup: int = 3, tuning: dict | 
             "plain_frames_per_s": round(1000.0 / plain_t, 3), "batched_frames_per_s": round(1000.0 / batch_t, 3),
             "speedup": round(plain_t / batch_t, 3), "batched_mtri_per_s": round(batch.num_tris / batch_t / 1e3, 2),
             "bit_exact_vs_plain": bool(exact), "overflow": counters["overflow"], "tuning": tuning or {}}
+
+
+# ---------------------------------------------------------------- fly-through
+WATER_CLEAR = (0.05, 0.1, 0.2, 1.0, 1.0)
+
+
+class FlyThrough:
+    """Camera fly-through over an n x n heightfield (2(n-1)^2 triangles) at
+    width x height, depth LESS, followed every frame by a translucent water
+    layer with about `overlay_frac` of the terrain's triangle count drawn
+    src-over on the same surfaces. Each frame runs the vertex stage on the
+    GPU (cr_vertex_shader_passthrough) into one of three vertex buffers, then
+    the opaque draw (with a deferred clear) and the overlay draw into one of
+    two colour/depth surface pairs."""
+
+    VERTEX_SLOTS = 3
+    TARGETS = 2
+
+    def __init__(self, n: int = 4096, width: int = 3840, height: int = 2160, frames: int = 300, seed: int = 5,
+                 overlay_frac: float = 0.1, water_level: float = -0.02, water_alpha: float = 0.35):
+        import math
+        p = _pkg()
+        scenes = importlib.import_module(PKG + ".scenes")
+        self.raster = importlib.import_module(PKG + ".raster")
+        self.scenes = scenes
+        self.n, self.width, self.height, self.frames = n, width, height, frames
+        pos, rgba, tris = scenes.grid_mesh(n, seed)
+        m = max(2, int(round((n - 1) * math.sqrt(overlay_frac))) + 1)
+        wpos, wrgba, wtris = scenes.water_mesh(m, water_level, water_alpha)
+        dev = "cuda"
+        self.layers = []
+        for name, pp, cc, tt in (("terrain", pos, rgba, tris), ("water", wpos, wrgba, wtris)):
+            self.layers.append({
+                "name": name,
+                "model": torch.from_numpy(np.ascontiguousarray(pp, dtype=np.float32)).to(dev),
+                "colors": torch.from_numpy(np.ascontiguousarray(cc, dtype=np.float32)).to(dev),
+                "indices": torch.from_numpy(np.ascontiguousarray(tt, dtype=np.int32)).to(dev),
+                "num_tris": int(tt.shape[0]),
+                "vbuf": [torch.empty((pp.shape[0], 8), dtype=torch.float32, device=dev)
+                         for _ in range(self.VERTEX_SLOTS)],
+            })
+        self.targets = [(p.CudaSurface((width, height), p.CudaSurface.FORMAT_RGBA8, 1),
+                         p.CudaSurface((width, height), p.CudaSurface.FORMAT_DEPTH32, 1)) for _ in range(self.TARGETS)]
+        self.mvps = [scenes.terrain_camera(f, width, height).astype(np.float32) for f in range(frames)]
+        self.num_tris = sum(layer["num_tris"] for layer in self.layers)
+
+    def camera_delta(self, a: int, b: int) -> np.ndarray:
+        return self.scenes.camera_delta(a, b)
+
+    def contexts(self, tuning: dict | None = None):
+        """One CudaRaster per layer (each keeps its own queues and counters)."""
+        p = _pkg()
+        out = []
+        for k, layer in enumerate(self.layers):
+            cr = p.CudaRaster()
+            cr.init()
+            if tuning:
+                cr.setTuning(**tuning)
+            cr.setSurfaces(*self.targets[0])
+            cr.setPixelPipe(None, "PixelPipe_gouraud" if k == 0 else "PixelPipe_gouraud_srcover")
+            cr.setIndexBuffer(layer["indices"], 0, layer["num_tris"])
+            out.append(cr)
+        return out
+
+    def transform(self, frame: int, stream=None) -> None:
+        slot = frame % self.VERTEX_SLOTS
+        for layer in self.layers:
+            self.raster.vertex_shader_passthrough(layer["model"], self.mvps[frame], layer["colors"],
+                                                  out=layer["vbuf"][slot], stream=stream)
+
+    def draw_layer(self, cr, k: int, frame: int, stream, sync: bool = True) -> None:
+        """Layer k of `frame` (0: opaque terrain with the deferred clear, 1:
+        water) from the frame's vertex slot into its surface pair."""
+        color, depth = self.target(frame)
+        cr.setSurfaces(color, depth)
+        cr.setVertexBuffer(self.layers[k]["vbuf"][frame % self.VERTEX_SLOTS], 0)
+        if k == 0:
+            cr.deferredClear(WATER_CLEAR[:4], WATER_CLEAR[4])
+        if sync:
+            cr.drawTriangles(stream)
+        else:
+            cr.drawTrianglesAsync(stream)
+
+    def draw(self, crs, frame: int, stream, sync: bool = True) -> None:
+        """Opaque terrain then the water layer of `frame`."""
+        for k, cr in enumerate(crs):
+            self.draw_layer(cr, k, frame, stream, sync)
+
+    def target(self, frame: int):
+        return self.targets[frame % self.TARGETS]
+
+    def frame_plain(self, crs, frame: int, stream) -> None:
+        self.transform(frame, stream)
+        self.draw(crs, frame, stream, sync=True)
+
+    def checksum(self, frame: int) -> int:
+        """64-bit position-weighted sum of the colour and depth words of the
+        surfaces `frame` was drawn into (enqueued on the current stream)."""
+        color, depth = self.target(frame)
+        if not hasattr(self, "_weights"):
+            n = color.tensor.numel()
+            idx = torch.arange(n, dtype=torch.int64, device="cuda")
+            self._weights = (idx * 2654435761 + 12345) % 2147483647 + 1
+        c = color.tensor.view(-1).to(torch.int64) & 0xFFFFFFFF
+        d = depth.tensor.view(-1).to(torch.int64) & 0xFFFFFFFF
+        return int(((c * self._weights).sum() + (d * self._weights.flip(0)).sum()).item())
+
+    def snapshot(self, frame: int):
+        color, depth = self.target(frame)
+        return color.tensor.clone(), depth.tensor.clone()
+
+
+def run_flythrough_plain(ft: FlyThrough, frames: range, tuning: dict | None = None, checksums: bool = False,
+                         keep: tuple = ()):
+    """The reference's usage: per frame, the vertex stage and two synchronous
+    drawTriangles calls. Returns (wall seconds, per-frame checksums, kept
+    frames, final counters)."""
+    import time
+    stream = torch.cuda.current_stream()
+    crs = ft.contexts(tuning)
+    sums, kept = [], {}
+    torch.cuda.synchronize()
+    wall = 0.0
+    for f in frames:
+        t0 = time.perf_counter()
+        ft.frame_plain(crs, f, stream)
+        torch.cuda.synchronize()
+        wall += time.perf_counter() - t0
+        if checksums:
+            sums.append(ft.checksum(f))
+        if f in keep:
+            kept[f] = ft.snapshot(f)
+    counters = [cr.getCounters() for cr in crs]
+    return wall, sums, kept, counters
+
+
+def run_flythrough_predicted(ft: FlyThrough, frames: int, train_frames: int = 50, tuning: dict | None = None,
+                             checksums: bool = False, keep: tuple = (), train_steps: int = 4,
+                             online_every: int = 4, seed: int = 0, lr: float = 3e-4, ahead: int = 2,
+                             min_margin: float = 0.02, margin_factor: float = 2.0):
+    """The first `train_frames` frames are plain (synchronous draws) and train
+    one predictor per layer on the counts they emit. Later frames are drawn
+    asynchronously into queues sized from predictions made `ahead` (= 2)
+    frames earlier, so the host keeps one frame queued: at frame f it judges
+    frame f - 2 (its overflow flags), then sizes and launches frame f. Each
+    layer's predictor step runs on its own stream right after that layer's
+    draw, and the next draw of the layer waits for it. A frame whose queues
+    overflowed is redrawn through the plain overflow-detect-and-rerun path (on
+    separate contexts, so the queued frame's counts survive) before its
+    surfaces are reused, and the predictor steps are redone. Returns wall
+    times, misses and the per-frame record."""
+    import time
+    if ahead != 2:
+        raise ValueError("the pipelined loop predicts two frames ahead")
+    P = importlib.import_module(PKG + ".predictor")
+    S = torch.cuda.current_stream()
+    L = len(ft.layers)
+    Q = [torch.cuda.Stream() for _ in range(L)]
+    crs = ft.contexts(tuning)
+    fallback = ft.contexts(tuning)
+    preds = None
+    R = ahead + 2
+    ev_draw = [[torch.cuda.Event() for _ in range(R)] for _ in range(L)]
+    ev_pred = [[torch.cuda.Event() for _ in range(R)] for _ in range(L)]
+    sums, kept, rec, launched = {}, {}, [], {}
+    wall_train, wall_pred, wait = 0.0, 0.0, 0.0
+    misses = [0] * L
+    extra = [0] * L             # most clip-generated subtriangles seen per layer
+
+    def draw_and_step(cset, f, sync, prev=None):
+        """Draw both layers of frame f; after each, its predictor step on its
+        stream. prev: the frame whose step must finish before a layer's
+        contexts are drawn again."""
+        for k, cr in enumerate(cset):
+            if prev is not None:
+                S.wait_event(ev_pred[k][prev % R])
+            ft.draw_layer(cr, k, f, S, sync)
+            if preds is None:
+                return
+            ev_draw[k][f % R].record(S)
+            Q[k].wait_event(ev_draw[k][f % R])
+            preds[k].step(cr, f, ft.camera_delta(f, f + ahead), Q[k])
+            ev_pred[k][f % R].record(Q[k])
+
+    def present(f):
+        if checksums:
+            sums[f] = ft.checksum(f)
+        if f in keep:
+            kept[f] = ft.snapshot(f)
+
+    def judge(f):
+        """Frame f's steps have completed; redraw it if a queue overflowed."""
+        ctr = [pr.counters_of(f) for pr in preds]
+        missed = [int(c[5]) != 0 for c in ctr]
+        if any(missed):
+            for k, m in enumerate(missed):
+                misses[k] += int(m)
+            torch.cuda.synchronize()
+            draw_and_step(fallback, f, True)        # the plain path: grows its queues and reruns until done
+            if f + 1 in launched:
+                for k, cr in enumerate(crs):        # frame f+1's trend used frame f's counts
+                    preds[k].step(cr, f + 1, ft.camera_delta(f + 1, f + 1 + ahead), Q[k])
+            torch.cuda.synchronize()
+        for k, pr in enumerate(preds):
+            c = pr.counters_of(f)
+            extra[k] = max(extra[k], int(c[0]))
+            if f in launched:
+                pt, cb, ct, pb = launched[f][k]
+                actual = (float(c[1]), float(c[3]))
+                pr.score(pt, actual)
+                rec.append({"frame": f, "layer": k, "pred_bin": pt[0], "pred_tile": pt[1], "perbin_bin": pb[0],
+                            "perbin_tile": pb[1], "cap_bin": cb, "cap_tile": ct, "bin": actual[0],
+                            "tile": actual[1], "miss": bool(missed[k])})
+        present(f)
+
+    torch.cuda.synchronize()
+    ft.transform(0, S)
+    for f in range(train_frames):
+        # Plain frames, drawn on the contexts that later serve the reruns.
+        t0 = time.perf_counter()
+        if preds is None:
+            ft.draw(fallback, f, S, sync=True)
+            preds = [P.QueuePredictor(P.queue_layout(cr), ahead=ahead, seed=seed + k, lr=lr,
+                                      min_margin=min_margin, margin_factor=margin_factor)
+                     for k, cr in enumerate(fallback)]
+            for k, cr in enumerate(fallback):
+                preds[k].step(cr, f, ft.camera_delta(f, f + ahead), Q[k])
+                ev_pred[k][f % R].record(Q[k])
+        else:
+            draw_and_step(fallback, f, True, prev=f - 1)
+        ft.transform(f + 1, S)
+        for k, pr in enumerate(preds):
+            pr.train(train_steps, f, Q[k])
+        torch.cuda.synchronize()
+        wall_train += time.perf_counter() - t0
+        for k, pr in enumerate(preds):
+            extra[k] = max(extra[k], int(pr.counters_of(f)[0]))
+        present(f)
+
+    t0 = time.perf_counter()
+    for f in range(train_frames, frames + ahead):
+        j = f - ahead                    # the frame to judge now
+        tw = time.perf_counter()
+        for k in range(L):
+            ev_pred[k][j % R].synchronize()
+        wait += time.perf_counter() - tw
+        if j >= train_frames:
+            judge(j)
+        if f >= frames:
+            continue
+        caps = []
+        for k, (pr, cr, layer) in enumerate(zip(preds, crs, ft.layers)):
+            pt = pr.predicted_totals(f)
+            cb, ct = pr.capacity(pt)
+            cr.setCapacity(layer["num_tris"] + max(4096, 2 * extra[k]), cb, ct)
+            caps.append((pt, cb, ct, pr.per_bin_totals(f)))
+        launched[f] = caps
+        draw_and_step(crs, f, False, prev=f - 1)
+        if f + 1 < frames:
+            ft.transform(f + 1, S)
+        if (f - train_frames) % online_every == 0:
+            for k, pr in enumerate(preds):
+                pr.train(1, j, Q[k])
+    torch.cuda.synchronize()
+    wall_pred = time.perf_counter() - t0
+    steps = [pr.net.steps for pr in preds or []]
+    for pr in preds or []:
+        pr.close()
+    return {"wall_train": wall_train, "wall_pred": wall_pred, "wait": wait, "misses": misses, "records": rec,
+            "checksums": [sums[f] for f in sorted(sums)], "kept": kept, "train_frames": train_frames,
+            "adam_steps": steps}

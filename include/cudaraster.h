@@ -217,6 +217,117 @@ cr_status cr_vertex_shader_passthrough(const float* model, int32_t model_stride,
                                        int32_t color_stride, void* out_vertices, int32_t out_stride_bytes,
                                        int64_t num_vertices, const float* mvp_row_major, void* stream);
 
+/* ---- Queue occupancy and the learned queue predictor ----
+ * No reference counterpart: the reference sizes its queues from the previous
+ * draw and grows them on overflow (CudaRaster.cpp:263-275, 325-342), which
+ * stays the fallback and the judge of every prediction made here. */
+
+/* Bin and tile grid of the last draw (of its first instance for a batch). */
+typedef struct cr_queue_layout {
+    int32_t bins_x, bins_y;       /* bins of (8 << bin_log2) pixels */
+    int32_t tiles_x, tiles_y;     /* 8x8-pixel tiles                */
+    int32_t bin_log2;
+    int32_t num_bins, num_tiles;  /* totals over all instances      */
+    int32_t num_instances;
+} cr_queue_layout;
+cr_status cr_get_queue_layout(cr_context* ctx, cr_queue_layout* out);
+/* Device pointers to the last draw's per-bin counts [num_bins], per-tile
+ * counts [num_tiles] and 8 counters, valid until the next draw on ctx. */
+cr_status cr_get_queue_buffers(cr_context* ctx, const int32_t** bin_counts, const int32_t** tile_counts,
+                               const int32_t** counters);
+
+/* Device-to-device copies, ordered on `stream` after the last draw, of its
+ * per-bin bin-queue entry counts [num_bins], per-tile tile-queue entry counts
+ * [num_tiles] and its 8 device counters (extra subtriangles, bin entries,
+ * coarse units, tile entries, fine tiles taken, overflow flags, 2 reserved).
+ * Any of the three pointers may be NULL. After an overflow the counts of the
+ * overflowing stage and later ones are incomplete. */
+cr_status cr_queue_counts(cr_context* ctx, int32_t* bin_counts, int32_t num_bins, int32_t* tile_counts,
+                          int32_t num_tiles, int32_t* counters, void* stream);
+
+/* Predictor input: x[cy*16+cx] = 0.125 * mean of log1p(count) over the bins
+ * (bx, by) with bx*16/bins_x == cx and by*16/bins_y == cy, x[256..261] =
+ * camera_delta (6 host floats). x: 262 device floats. */
+cr_status cr_queue_features(const int32_t* bin_counts, int32_t bins_x, int32_t bins_y, const float* camera_delta,
+                            float* x, void* stream);
+/* logs[b] = log1p(bin entries of bin b), logs[nb + b] = log1p(sum of the tile
+ * entries of bin b's tiles), logs[2nb] / logs[2nb + 1] = log1p of the bin /
+ * tile entry totals; nb = bins_x * bins_y. logs: 2nb + 6 device floats,
+ * 8-byte aligned (the last four are scratch for the 64-bit totals). */
+cr_status cr_queue_log_counts(const int32_t* bin_counts, const int32_t* tile_counts, int32_t bins_x, int32_t bins_y,
+                              int32_t tiles_x, int32_t tiles_y, int32_t bin_log2, float* logs, void* stream);
+/* The network's regression target: target[i] = logs_cur[i] - logs_prev[i],
+ * minus (logs_prev[i] - logs_prevprev[i]) for the last n_trend entries when
+ * logs_prevprev is given (the total heads learn corrections to the trend). */
+cr_status cr_queue_targets(const float* logs_prevprev, const float* logs_prev, const float* logs_cur, int32_t n,
+                           int32_t n_trend, float* target, void* stream);
+/* Occupancy predicted from the last logs and the network output (2nb + 2
+ * values): per_bin[i] = max(expm1(logs_prev[i] + prediction[i]), 0) for
+ * i < 2nb (may be NULL); totals[0] / totals[1] = predicted bin / tile entry
+ * totals from the total heads, expm1(logs_prev[h] + (logs_prev[h] -
+ * logs_prevprev[h]) + prediction[h]) (no trend term when logs_prevprev is
+ * NULL); totals[2] / totals[3] = sums of the per-bin predictions (device
+ * doubles). */
+cr_status cr_queue_plan(const float* logs_prevprev, const float* logs_prev, const float* prediction,
+                        int32_t num_bins, float* per_bin, double* totals, void* stream);
+
+/* The network: inputs -> hidden1 -> hidden2 -> outputs, GELU after both
+ * hidden layers. Parameters are held in FP32 (Adam master copy) and used in
+ * BF16; every product is accumulated in FP32. Flat parameter layout:
+ * W1[hidden1][inputs], b1[hidden1], W2[hidden2][hidden1], b2[hidden2],
+ * W3[outputs][hidden2], b3[outputs]. Loss: mean squared error over the
+ * batch's outputs. A predictor's calls must be ordered (one stream): they
+ * share its activation buffers. All data pointers are device pointers. */
+typedef struct cr_predictor cr_predictor;
+cr_status cr_predictor_create(cr_predictor** out, int32_t inputs, int32_t hidden1, int32_t hidden2, int32_t outputs,
+                              int32_t max_batch);
+void      cr_predictor_destroy(cr_predictor* p);
+int64_t   cr_predictor_num_params(const cr_predictor* p);
+int64_t   cr_predictor_steps(const cr_predictor* p);
+/* Host FP32 parameters in; the BF16 copy is rounded to nearest even and the
+ * Adam state reset. Synchronous. */
+cr_status cr_predictor_set_params(cr_predictor* p, const float* host, int64_t n);
+cr_status cr_predictor_get_params(const cr_predictor* p, float* host, int64_t n);
+cr_status cr_predictor_get_params_bf16(const cr_predictor* p, uint16_t* host, int64_t n);
+/* y[batch][outputs] = network(x[batch][inputs]). */
+cr_status cr_predictor_forward(cr_predictor* p, const float* x, int32_t batch, float* y, void* stream);
+/* Gradients of the loss over rows `rows[0..batch)` of the sample pools of
+ * pool_rows rows each (rows NULL: rows 0..batch-1) into grads[num_params]
+ * (may be NULL) and the loss into *loss (device float, may be NULL);
+ * parameters unchanged. A row index outside the pool reads row 0 instead
+ * and raises the flag that cr_predictor_bad_rows returns. */
+cr_status cr_predictor_gradients(cr_predictor* p, const float* x_pool, const float* target_pool, int32_t pool_rows,
+                                 const int32_t* rows, int32_t batch, float* grads, float* loss, void* stream);
+/* One Adam step (bias-corrected) on the gradients of those rows. */
+cr_status cr_predictor_train_step(cr_predictor* p, const float* x_pool, const float* target_pool, int32_t pool_rows,
+                                  const int32_t* rows, int32_t batch, float lr, float beta1, float beta2, float eps,
+                                  float* loss, void* stream);
+/* One frame k of the online predictor in a single launch, for a network with
+ * 262 inputs (16x16 histogram + camera delta) and 2nb + 2 outputs predicting
+ * `ahead` frames on. From the draw's counts (bin_counts, tile_counts,
+ * counters: device pointers, e.g. from cr_get_queue_buffers) it writes
+ *   - logs_cur: frame k's logs (as cr_queue_log_counts, 2nb + 2 floats);
+ *   - target: the target of the sample that frame k completes, whose input
+ *     was frame k - ahead (logs_target_base; logs_target_trend = frame
+ *     k - ahead - 1, may be NULL): logs_cur - base, and for the two total
+ *     heads also - ahead * (base - trend); skipped when target or
+ *     logs_target_base is NULL (cr_queue_targets for ahead = 1);
+ *   - x_next[262]: frame k's pooled histogram and camera_delta_ahead (the
+ *     camera move from k to k + ahead), bit for bit as cr_queue_features;
+ *   - the network's prediction for frame k + ahead and its plan (as
+ *     cr_queue_plan with frame k as the base, the total heads on the trend
+ *     expm1(cur + ahead * (cur - logs_prev) + y); per_bin may be NULL);
+ *   - fetch (device, 64 bytes, 8-byte aligned): the 4 predicted totals
+ *     (doubles), then the draw's 8 counters (int32), for one copy to host. */
+cr_status cr_predictor_frame(cr_predictor* p, const int32_t* bin_counts, const int32_t* tile_counts,
+                             const int32_t* counters, const cr_queue_layout* layout, int32_t ahead,
+                             const float* logs_prev, float* logs_cur, const float* logs_target_base,
+                             const float* logs_target_trend, float* target, const float* camera_delta_ahead,
+                             float* x_next, float* per_bin, void* fetch, void* stream);
+/* *flag = nonzero if a batch since the last reset named a row outside its
+ * pool; reset != 0 clears it. Synchronous. */
+cr_status cr_predictor_bad_rows(cr_predictor* p, int32_t* flag, int32_t reset);
+
 /* ---- Results ---- */
 cr_status cr_get_stats(cr_context* ctx, cr_stats* out);
 cr_status cr_get_counters(cr_context* ctx, cr_counters* out);
