@@ -11,6 +11,13 @@ memory and the framebuffer copied back inside the timed region.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
+Two sub-objects compare the plain single-scene path with the batched and the
+predictor-sized paths, bit for bit: "batched" (64 uneven scenes drawn one by
+one vs one CUDA-graph replay of all of them) and "flythrough" (a 300-frame
+camera loop over a 4096^2 heightfield plus a translucent water layer at
+3840x2160: synchronous plain draws vs draws sized two frames ahead by the
+learned queue predictor and queued asynchronously).
+
 With --impl reference the CPU restatement of the reference pipeline (the
 oracle, OpenMP over all host cores) renders the same scene; under torchrun
 only rank 0 runs it.
@@ -153,6 +160,32 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+FLY_ORACLE_FRAME = 150
+
+
+def flythrough_oracle_check(ft, kept, f):
+    """One fly-through frame of the plain pass against the CPU oracle (both
+    layers, all host cores)."""
+    import time
+    from oracle import oracle as orc
+    raster = importlib.import_module(PKG + ".raster")
+    pkg = importlib.import_module(PKG)
+    workloads = importlib.import_module(PKG + ".workloads")
+    t0 = time.perf_counter()
+    clear = (pkg.color_to_abgr(*workloads.WATER_CLEAR[:4]), pkg.clear_depth_from_float(workloads.WATER_CLEAR[4]))
+    color = depth = None
+    for k, layer in enumerate(ft.layers):
+        clip = raster.vertex_shader_reference(layer["model"].cpu().numpy(), ft.mvps[f])
+        verts = np.concatenate([clip, layer["colors"].cpu().numpy()], axis=1).astype(np.float32)
+        p = orc.make_pipe(ft.width, ft.height, 1, orc.DEPTH | orc.LERP, "replace" if k == 0 else "srcover",
+                          "gouraud", 32, clear if k == 0 else None)
+        color, depth, _ = orc.render(p, verts, layer["indices"].cpu().numpy(), color, depth, 0)
+    gc = kept[f][0].cpu().numpy().view(np.uint32)
+    gd = kept[f][1].cpu().numpy().view(np.uint32)
+    return {"frame": f, "bit_exact": bool((gc == color).all() and (gd == depth).all()),
+            "oracle_s": round(time.perf_counter() - t0, 1)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -161,6 +194,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the uneven-batch comparison")
+    ap.add_argument("--no-flythrough", action="store_true", help="skip the fly-through with the queue predictor")
     ap.add_argument("--profile-frames", type=int, default=0,
                     help="only draw this many frames of the workload (for ncu captures), print nothing else")
     args = ap.parse_args()
@@ -321,12 +355,18 @@ def main():
                                workload="uneven batch: 64 random soups, 1k-500k triangles (log-uniform), "
                                         "resolutions 256^2..1920x1080, half src-over blended; "
                                         "plain = 64 sequential drawTriangles, batched = one CUDA-graph replay")
+    fly = None
+    if rank == 0 and not args.no_flythrough:
+        fly = workloads.measure_flythrough(tuning=tuning, keep=(FLY_ORACLE_FRAME,))
+        line["flythrough"] = fly[0]
     if rank == 0 and not args.no_cpu_baseline:
         cb, (rc, rd, st) = cpu_baseline(sc)
         gc = color.download().numpy().astype(np.uint32)
         gd = depth.download().numpy().astype(np.uint32)
         line["cpu_baseline"] = cb
         line["bit_exact_vs_oracle"] = bool((gc == rc).all() and (gd == rd).all())
+        if fly is not None:
+            line["flythrough"]["oracle_frame"] = flythrough_oracle_check(fly[2], fly[1], FLY_ORACLE_FRAME)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -246,7 +246,7 @@ def run_flythrough_plain(ft: FlyThrough, frames: range, tuning: dict | None = No
 def run_flythrough_predicted(ft: FlyThrough, frames: int, train_frames: int = 50, tuning: dict | None = None,
                              checksums: bool = False, keep: tuple = (), train_steps: int = 4,
                              online_every: int = 4, seed: int = 0, lr: float = 3e-4, ahead: int = 2,
-                             min_margin: float = 0.02, margin_factor: float = 2.0):
+                             min_margin: float = 0.02, margin_factor: float = 2.0, capacity_scale: float = 1.0):
     """The first `train_frames` frames are plain (synchronous draws) and train
     one predictor per layer on the counts they emit. Later frames are drawn
     asynchronously into queues sized from predictions made `ahead` (= 2)
@@ -256,8 +256,9 @@ def run_flythrough_predicted(ft: FlyThrough, frames: int, train_frames: int = 50
     draw, and the next draw of the layer waits for it. A frame whose queues
     overflowed is redrawn through the plain overflow-detect-and-rerun path (on
     separate contexts, so the queued frame's counts survive) before its
-    surfaces are reused, and the predictor steps are redone. Returns wall
-    times, misses and the per-frame record."""
+    surfaces are reused, and the predictor steps are redone. capacity_scale
+    (tests) scales the capacities given to the draws. Returns wall times,
+    misses and the per-frame record."""
     import time
     if ahead != 2:
         raise ValueError("the pipelined loop predicts two frames ahead")
@@ -360,7 +361,7 @@ def run_flythrough_predicted(ft: FlyThrough, frames: int, train_frames: int = 50
         caps = []
         for k, (pr, cr, layer) in enumerate(zip(preds, crs, ft.layers)):
             pt = pr.predicted_totals(f)
-            cb, ct = pr.capacity(pt)
+            cb, ct = (int(c * capacity_scale) for c in pr.capacity(pt))
             cr.setCapacity(layer["num_tris"] + max(4096, 2 * extra[k]), cb, ct)
             caps.append((pt, cb, ct, pr.per_bin_totals(f)))
         launched[f] = caps
@@ -378,3 +379,63 @@ def run_flythrough_predicted(ft: FlyThrough, frames: int, train_frames: int = 50
     return {"wall_train": wall_train, "wall_pred": wall_pred, "wait": wait, "misses": misses, "records": rec,
             "checksums": [sums[f] for f in sorted(sums)], "kept": kept, "train_frames": train_frames,
             "adam_steps": steps}
+
+
+FLYTHROUGH_WORKLOAD = ("fly-through: 4096^2 heightfield (33.5M triangles, 6-octave value noise) + translucent water "
+                       "layer (10% of the triangles, src-over) at 3840x2160, depth LESS, 300-frame camera loop; "
+                       "per frame the GPU vertex stage and two draws; frames 0-49 plain and training the predictor")
+
+
+def measure_flythrough(n: int = 4096, width: int = 3840, height: int = 2160, frames: int = 300,
+                       train_frames: int = 50, tuning: dict | None = None, keep: tuple = ()):
+    """Plain vs predictor-sized pipelined fly-through over the same frames.
+    Returns (summary dict, {frame: (colour, depth)} of the plain pass, the
+    FlyThrough)."""
+    ft = FlyThrough(n=n, width=width, height=height, frames=frames)
+    run_flythrough_plain(ft, range(3), tuning)                                   # warm-up
+    _, sums, kept, ctr = run_flythrough_plain(ft, range(frames), tuning, checksums=True, keep=keep)
+    exact = run_flythrough_predicted(ft, frames, train_frames, tuning, checksums=True)
+    wall_plain, _, _, _ = run_flythrough_plain(ft, range(train_frames, frames), tuning)
+    res = run_flythrough_predicted(ft, frames, train_frames, tuning)
+    n_pred = frames - train_frames
+    plain_fps = n_pred / wall_plain
+    pred_fps = n_pred / res["wall_pred"]
+    layers = []
+    for k, layer in enumerate(ft.layers):
+        r = sorted((x for x in res["records"] if x["layer"] == k), key=lambda x: x["frame"])
+        T = layer["num_tris"]
+        entry = {"layer": layer["name"], "triangles": T, "misses": res["misses"][k],
+                 "queue_mb_plain_estimate": round((2 * T + 65536 + 4 * T + 65536) * 4 / 2**20, 1),
+                 "queue_mb_predicted_mean": round(float(np.mean([x["cap_bin"] + x["cap_tile"] for x in r])) * 4 / 2**20,
+                                                  1),
+                 "queue_mb_predicted_max": round(float(np.max([x["cap_bin"] + x["cap_tile"] for x in r])) * 4 / 2**20,
+                                                 1),
+                 "queue_mb_used_max": round(float(np.max([x["bin"] + x["tile"] for x in r])) * 4 / 2**20, 1)}
+        errs = {}
+        for q in ("bin", "tile"):
+            a = np.array([x[q] for x in r])
+            p = np.array([x["pred_" + q] for x in r])
+            # frame f is sized at frame f - 2: previous-frame sizing uses a[f-2],
+            # trend extrapolation a[f-2] * (a[f-2] / a[f-3])^2.
+            prev = a[1:-2]
+            trend = a[1:-2] ** 3 / a[:-3] ** 2
+            tgt = a[3:]
+            errs[q] = {"predictor": round(float(np.abs(np.log(tgt / p[3:])).mean()), 5),
+                       "previous_frame": round(float(np.abs(np.log(tgt / prev)).mean()), 5),
+                       "trend_only": round(float(np.abs(np.log(tgt / trend)).mean()), 5),
+                       "predictor_max": round(float(np.abs(np.log(tgt / p[3:])).max()), 5),
+                       "previous_frame_max": round(float(np.abs(np.log(tgt / prev)).max()), 5)}
+        entry["mean_abs_log_error"] = errs
+        layers.append(entry)
+    summary = {"workload": FLYTHROUGH_WORKLOAD, "frames": frames, "train_frames": train_frames,
+               "triangles_per_frame": ft.num_tris, "plain_frames_per_s": round(plain_fps, 2),
+               "predicted_frames_per_s": round(pred_fps, 2), "speedup": round(pred_fps / plain_fps, 3),
+               "plain_mtri_per_s": round(ft.num_tris * plain_fps / 1e6, 1),
+               "predicted_mtri_per_s": round(ft.num_tris * pred_fps / 1e6, 1),
+               "bit_exact_vs_plain": exact["checksums"] == sums, "frames_checked": len(sums),
+               "misses": res["misses"], "miss_rate": round(sum(res["misses"]) / (2 * n_pred), 4),
+               "adam_steps": res["adam_steps"], "layers": layers,
+               "plain": "vertex stage + two synchronous drawTriangles per frame",
+               "predicted": "queues sized by the predictor two frames ahead, draws queued asynchronously, "
+                            "one judge per frame, misses redrawn by the plain path"}
+    return summary, kept, ft
