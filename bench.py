@@ -186,6 +186,22 @@ def flythrough_oracle_check(ft, kept, f):
             "oracle_s": round(time.perf_counter() - t0, 1)}
 
 
+def subpixel_oracle_check(sc, got):
+    """The 4x MSAA heightfield frame against the CPU oracle (all host cores)."""
+    import time
+    from oracle import oracle as orc
+    pkg = importlib.import_module(PKG)
+    workloads = importlib.import_module(PKG + ".workloads")
+    t0 = time.perf_counter()
+    clear = (pkg.color_to_abgr(*workloads.CLEAR[:4]), pkg.clear_depth_from_float(workloads.CLEAR[4]))
+    p = orc.make_pipe(sc["width"], sc["height"], sc["samples"], orc.DEPTH | orc.LERP, "replace", "gouraud", 32, clear)
+    rc, rd, st = orc.render(p, sc["vertices"], sc["indices"], None, None, 0)
+    gc = got[0].cpu().numpy().view(np.uint32)
+    gd = got[1].cpu().numpy().view(np.uint32)
+    return {"bit_exact": bool((gc == rc).all() and (gd == rd).all()), "zmin_violations": st["zmin_violations"],
+            "oracle_s": round(time.perf_counter() - t0, 1)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -195,6 +211,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the uneven-batch comparison")
     ap.add_argument("--no-flythrough", action="store_true", help="skip the fly-through with the queue predictor")
+    ap.add_argument("--no-subpixel", action="store_true", help="skip the 4x MSAA grazing-heightfield frame")
     ap.add_argument("--profile-frames", type=int, default=0,
                     help="only draw this many frames of the workload (for ncu captures), print nothing else")
     args = ap.parse_args()
@@ -355,6 +372,10 @@ def main():
                                workload="uneven batch: 64 random soups, 1k-500k triangles (log-uniform), "
                                         "resolutions 256^2..1920x1080, half src-over blended; "
                                         "plain = 64 sequential drawTriangles, batched = one CUDA-graph replay")
+    sub = None
+    if rank == 0 and not args.no_subpixel:
+        sub = workloads.measure_subpixel(tuning=tuning)
+        line["subpixel_stress"] = sub[0]
     fly = None
     if rank == 0 and not args.no_flythrough:
         fly = workloads.measure_flythrough(tuning=tuning, keep=(FLY_ORACLE_FRAME,))
@@ -367,6 +388,8 @@ def main():
         line["bit_exact_vs_oracle"] = bool((gc == rc).all() and (gd == rd).all())
         if fly is not None:
             line["flythrough"]["oracle_frame"] = flythrough_oracle_check(fly[2], fly[1], FLY_ORACLE_FRAME)
+        if sub is not None:
+            line["subpixel_stress"]["oracle"] = subpixel_oracle_check(sub[2], sub[1])
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -17,55 +17,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "Types.hpp"
+
 namespace FW {
-
-typedef int8_t S8;
-typedef uint8_t U8;
-typedef int16_t S16;
-typedef uint16_t U16;
-typedef int32_t S32;
-typedef uint32_t U32;
-typedef int64_t S64;
-typedef uint64_t U64;
-typedef float F32;
-typedef double F64;
-
-// ------------------------------------------------------------ vector types
-struct Vec2i {
-    S32 x, y;
-    __host__ __device__ Vec2i() : x(0), y(0) {}
-    __host__ __device__ Vec2i(S32 a, S32 b) : x(a), y(b) {}
-};
-struct Vec3i {
-    S32 x, y, z;
-    __host__ __device__ Vec3i() : x(0), y(0), z(0) {}
-    __host__ __device__ Vec3i(S32 a, S32 b, S32 c) : x(a), y(b), z(c) {}
-    __host__ __device__ S32& operator[](int i) { return (&x)[i]; }
-    __host__ __device__ const S32& operator[](int i) const { return (&x)[i]; }
-};
-struct Vec2f {
-    F32 x, y;
-    __host__ __device__ Vec2f() : x(0), y(0) {}
-    __host__ __device__ Vec2f(F32 a) : x(a), y(a) {}
-    __host__ __device__ Vec2f(F32 a, F32 b) : x(a), y(b) {}
-};
-struct Vec3f {
-    F32 x, y, z;
-    __host__ __device__ Vec3f() : x(0), y(0), z(0) {}
-    __host__ __device__ Vec3f(F32 a) : x(a), y(a), z(a) {}
-    __host__ __device__ Vec3f(F32 a, F32 b, F32 c) : x(a), y(b), z(c) {}
-    __host__ __device__ F32& operator[](int i) { return (&x)[i]; }
-    __host__ __device__ const F32& operator[](int i) const { return (&x)[i]; }
-};
-struct Vec4f {
-    F32 x, y, z, w;
-    __host__ __device__ Vec4f() : x(0), y(0), z(0), w(0) {}
-    __host__ __device__ Vec4f(F32 a) : x(a), y(a), z(a), w(a) {}
-    __host__ __device__ Vec4f(F32 a, F32 b, F32 c, F32 d) : x(a), y(b), z(c), w(d) {}
-    __host__ __device__ Vec4f(const Vec3f& v, F32 d) : x(v.x), y(v.y), z(v.z), w(d) {}
-    __host__ __device__ F32& operator[](int i) { return (&x)[i]; }
-    __host__ __device__ const F32& operator[](int i) const { return (&x)[i]; }
-};
 
 // Component-wise arithmetic, each operation rounded on its own (no FMA
 // contraction), as the reference source reads.
