@@ -142,6 +142,23 @@ def cpu_baseline(sc, budget_s: float = 12.0, min_frames: int = 1):
             "mtri_per_s": frames * sc["indices"].shape[0] / el / 1e6}, out
 
 
+def reduce_max(x: float, world: int, device="cuda") -> float:
+    """The largest x over the ranks (one all-reduce; x itself for one rank)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world: int, steps: int, total_ms: float) -> float:
+    """Frames per second of N independent replicas that each drew `steps`
+    frames, the slowest in `total_ms` (weak scaling: work grows with N)."""
+    return world * steps / (total_ms / 1e3)
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -283,12 +300,9 @@ def main():
         dist.barrier()
     step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
     total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = reduce_max(total_ms, world, "cuda")
     ms_per_step = total_ms / args.steps
-    value = world * args.steps / (total_ms / 1e3)
+    value = replica_throughput(world, args.steps, total_ms)
     stage_ms = stage / args.steps * 1e3
     counters = cr.getCounters()
 
@@ -323,11 +337,8 @@ def main():
         torch.cuda.synchronize()
         e2e_ms.append(a.elapsed_time(b))
     e2e_total = sum(e2e_ms)
-    if world > 1:
-        t = torch.tensor([e2e_total], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_total = float(t.item())
-    e2e_value = world * args.steps / (e2e_total / 1e3)
+    e2e_total = reduce_max(e2e_total, world, "cuda")
+    e2e_value = replica_throughput(world, args.steps, e2e_total)
     h2d = hv.numel() * 4 + hi.numel() * 4
     d2h = (hc.numel() + hd.numel()) * 4
 
