@@ -60,13 +60,17 @@ __device__ __forceinline__ int cellIndex(const Grid& gr, S32 cx, S32 cy) {
     return (cy - gr.cy0) * gr.stride + (cx - gr.cx0);
 }
 
-// Items too large for their own thread, walked by a whole warp.
+// Items too large for their own thread, walked by a whole warp. Vertices and
+// box corners are kept as 16-bit pairs (snapped coordinates are S16, cell
+// coordinates below 2^15).
 struct BigItem {
-    TriGeom g;
-    CellBox box;
-    S32 who;     // threadIdx.x of the item's owner (warp * 32 + lane)
+    U32 v[3];    // (x, y) of each vertex as in the triangle header
+    U32 lo, hi;  // box corners (lx, ly), (hx, hy)
     U32 entry;
+    S32 who;     // threadIdx.x of the item's owner (warp * 32 + lane)
 };
+
+__device__ __forceinline__ U32 pack16(S32 a, S32 b) { return ((U32)a & 0xFFFFu) | ((U32)b << 16); }
 
 struct RoundShared {
     BigItem big[kBinThreads];
@@ -91,10 +95,14 @@ __device__ __forceinline__ void visitRound(RoundShared& rs, bool valid, const Tr
         __syncthreads();
         if (n > kSmallCells) {
             int k = atomicAdd(&rs.numBig, 1);
-            rs.big[k].g = g;
-            rs.big[k].box = box;
-            rs.big[k].who = threadIdx.x;
-            rs.big[k].entry = entry;
+            BigItem& it = rs.big[k];
+            it.v[0] = pack16(g.x0, g.y0);
+            it.v[1] = pack16(g.x1, g.y1);
+            it.v[2] = pack16(g.x2, g.y2);
+            it.lo = pack16(box.lx, box.ly);
+            it.hi = pack16(box.hx, box.hy);
+            it.who = threadIdx.x;
+            it.entry = entry;
         }
     }
     if (n > 0 && n <= kSmallCells) {
@@ -107,15 +115,19 @@ __device__ __forceinline__ void visitRound(RoundShared& rs, bool valid, const Tr
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int b = warp; b < nb; b += kBinWarps) {
         const BigItem& it = rs.big[b];
-        const S32 w = it.box.hx - it.box.lx + 1;
-        const S32 cnt = it.box.count();
+        const TriGeom bg = geomFromHeader(make_uint4(it.v[0], it.v[1], it.v[2], 0u));
+        const CellBox bb{lo16(it.lo), hi16(it.lo), lo16(it.hi), hi16(it.hi)};
+        const S32 who = it.who;
+        const U32 e = it.entry;
+        const S32 w = bb.hx - bb.lx + 1;
+        const S32 cnt = bb.count();
         // Cell c of the box is (c % w, c / w); the quotient is taken in
         // binary32, exact here because c < 2^11 and w <= 2^5.
         const F32 invW = 1.0f / (F32)w;
         for (S32 c = lane; c < cnt; c += 32) {
             const S32 q = (S32)(((F32)c + 0.5f) * invW);
-            const S32 cx = it.box.lx + (c - q * w), cy = it.box.ly + q;
-            if (cellTouched(it.g, it.box, cx, cy, gr.halfW, gr.halfH, gr.cellLog2)) fn(cellIndex(gr, cx, cy), it.who, it.entry);
+            const S32 cx = bb.lx + (c - q * w), cy = bb.ly + q;
+            if (cellTouched(bg, bb, cx, cy, gr.halfW, gr.halfH, gr.cellLog2)) fn(cellIndex(gr, cx, cy), who, e);
         }
     }
 }
@@ -133,20 +145,66 @@ __device__ __forceinline__ Grid binGrid(const InstanceDev* in, int binLog2) {
     return gr;
 }
 
-// Items of a bin-stage round: triangles [r0, r0 + 512) of the chunk expanded
-// into their subtriangles, in (triangle, subtriangle) order.
-struct ItemRound {
-    S32 m;  // number of items
-};
+// The chunk's subtriangle items stream through a window in shared memory
+// (kWindow entries), so that every round holds up to kBinThreads live items:
+// culled triangles carry none. Items keep (triangle, subtriangle) order.
+constexpr int kWindow = kBinThreads * (kMaxSubtrisPerTri + 1);
 
-__device__ __forceinline__ ItemRound expandRound(const DrawDev& d, S64 r0, S64 t1, U32* s_items, S32* s_scratch) {
-    S64 t = r0 + threadIdx.x;
-    int n = (t < t1) ? d.triSubtris[t] : 0;
-    S32 m;
-    S32 pos = blockExclusiveScan(n, s_scratch, &m);
-    for (int s = 0; s < n; s++) s_items[pos + s] = ((U32)t << 3) | (U32)(n == 1 ? 7 : s);
-    __syncthreads();
-    return ItemRound{m};
+// Appends the items of the next triangles of [next, t1) until the window
+// holds at least kBinThreads items or the chunk is exhausted. Each thread
+// takes kRefillTris consecutive triangles; if their items would overflow the
+// window only the first kBinThreads triangles are taken (at most 7 items
+// each, which always fit). fill and next are uniform across the CTA.
+constexpr int kRefillTris = 4;
+
+__device__ __forceinline__ S32 refillWindow(const DrawDev& d, S64& next, S64 t1, S32 fill, U32* s_items,
+                                            S32* s_scratch) {
+    __shared__ S32 s_cut;
+    while (fill < kBinThreads && next < t1) {
+        const S64 t = next + (S64)threadIdx.x * kRefillTris;
+        int n[kRefillTris];
+        int sum = 0;
+#pragma unroll
+        for (int j = 0; j < kRefillTris; j++) {
+            n[j] = (t + j < t1) ? d.triSubtris[t + j] : 0;
+            sum += n[j];
+        }
+        if (!__syncthreads_or(sum)) {
+            next += kBinThreads * kRefillTris;
+            continue;
+        }
+        S32 m;
+        const S32 pos = blockExclusiveScan(sum, s_scratch, &m);
+        // Items of the first kBinThreads triangles (threads below
+        // kBinThreads / kRefillTris) end where the next thread's begin.
+        if (threadIdx.x == kBinThreads / kRefillTris) s_cut = pos;
+        __syncthreads();
+        const bool all = fill + m <= kWindow;
+        const bool take = all || (int)threadIdx.x < kBinThreads / kRefillTris;
+        if (take) {
+            S32 p = fill + pos;
+#pragma unroll
+            for (int j = 0; j < kRefillTris; j++)
+                for (int s = 0; s < n[j]; s++) s_items[p++] = ((U32)(t + j) << 3) | (U32)(n[j] == 1 ? 7 : s);
+        }
+        fill += all ? m : s_cut;
+        next += all ? (S64)kBinThreads * kRefillTris : (S64)kBinThreads;
+        __syncthreads();
+    }
+    return fill;
+}
+
+// Drops the kBinThreads items of the round just processed from the window.
+__device__ __forceinline__ S32 consumeWindow(U32* s_items, S32 fill) {
+    const S32 rest = fill - kBinThreads;
+    for (S32 i0 = 0; i0 < rest; i0 += kBinThreads) {
+        const S32 i = i0 + threadIdx.x;
+        const U32 v = (i < rest) ? s_items[kBinThreads + i] : 0u;
+        __syncthreads();
+        if (i < rest) s_items[i] = v;
+        __syncthreads();
+    }
+    return rest > 0 ? rest : 0;
 }
 
 // ------------------------------------------------------------------ bin
@@ -155,7 +213,7 @@ __device__ __forceinline__ ItemRound expandRound(const DrawDev& d, S64 r0, S64 t
 __global__ void __launch_bounds__(kBinThreads, 2) binCountKernel(DrawDev d) {
     extern __shared__ S32 s_count[];
     __shared__ RoundShared rs;
-    __shared__ U32 s_items[kBinThreads * kMaxSubtrisPerTri];
+    __shared__ U32 s_items[kWindow];
     __shared__ S32 s_scratch[kBinWarps + 1];
     __shared__ int s_inst;
     if (__ldg(&d.counters->overflow) & kOverflowSubtris) return;
@@ -171,20 +229,20 @@ __global__ void __launch_bounds__(kBinThreads, 2) binCountKernel(DrawDev d) {
     const S64 t0 = triBase + (S64)local * __ldg(&in->chunkTris);
     const S64 t1 = min(t0 + __ldg(&in->chunkTris), triBase + __ldg(&in->numTris));
     __syncthreads();
-    for (S64 r0 = t0; r0 < t1; r0 += kBinThreads) {
-        ItemRound ir = expandRound(d, r0, t1, s_items, s_scratch);
-        for (S32 k0 = 0; k0 < ir.m; k0 += kBinThreads) {
-            const S32 k = k0 + threadIdx.x;
-            const bool valid = k < ir.m;
-            TriGeom g{};
-            U32 entry = 0;
-            if (valid) {
-                entry = s_items[k];
-                g = geomFromHeader(d.triHeader[entrySlot(entry, d.triHeader)]);
-            }
-            visitRound(rs, valid, g, entry, gr, true, [&](int cell, S32, U32) { atomicAdd(&s_count[cell], 1); });
-            __syncthreads();
+    S64 next = t0;
+    for (S32 fill = 0;;) {
+        fill = refillWindow(d, next, t1, fill, s_items, s_scratch);
+        if (fill == 0) break;
+        const bool valid = (S32)threadIdx.x < fill;
+        TriGeom g{};
+        U32 entry = 0;
+        if (valid) {
+            entry = s_items[threadIdx.x];
+            g = geomFromHeader(d.triHeader[entrySlot(entry, d.triHeader)]);
         }
+        visitRound(rs, valid, g, entry, gr, true, [&](int cell, S32, U32) { atomicAdd(&s_count[cell], 1); });
+        __syncthreads();
+        fill = consumeWindow(s_items, fill);
     }
     __syncthreads();
     S32* out = d.chunkBinCount + __ldg(&in->chunkCountBase) + (S64)local * nb;
@@ -236,36 +294,93 @@ __global__ void __launch_bounds__(kBinThreads) binScanKernel(DrawDev d) {
     }
 }
 
-// Ranked scatter of one round of items into per-cell lists. s_mask/s_pre are
-// [kBinWarps][ncells]; s_run holds each cell's next free list index.
+// Per-cell scratch of a scatter CTA, carved from dynamic shared memory for
+// ncells cells: per-warp ballot masks and prefixes, each cell's next free list
+// index and round total, and the cells the current round touched (a bit per
+// cell and a list), so the per-round bookkeeping costs O(touched cells).
+struct ScatterSmem {
+    U32* mask;     // [kBinWarps][ncells]
+    S32* pre;      // [kBinWarps][ncells]
+    S32* run;      // [ncells]
+    S32* tot;      // [ncells]
+    U32* touched;  // [(ncells + 31) / 32]
+    S32* ntouch;   // [1]
+    uint16_t* list;     // [ncells]
+    int ncells;
+};
+
+__host__ __device__ inline size_t scatterSmemBytes(int ncells) {
+    return sizeof(S32) * ((size_t)2 * kBinWarps * ncells + 2 * ncells + (ncells + 31) / 32 + 1) +
+           sizeof(uint16_t) * (size_t)ncells;
+}
+
+__device__ __forceinline__ ScatterSmem carveScatter(S32* smem, int ncells) {
+    ScatterSmem sm;
+    sm.ncells = ncells;
+    sm.mask = (U32*)smem;
+    sm.pre = smem + kBinWarps * ncells;
+    sm.run = sm.pre + kBinWarps * ncells;
+    sm.tot = sm.run + ncells;
+    sm.touched = (U32*)(sm.tot + ncells);
+    sm.ntouch = (S32*)(sm.touched + (ncells + 31) / 32);
+    sm.list = (uint16_t*)(sm.ntouch + 1);
+    return sm;
+}
+
+// Zeroes masks and touch state (run is set by the caller). Ends with a barrier.
+__device__ __forceinline__ void clearScatter(const ScatterSmem& sm) {
+    for (int c = threadIdx.x; c < sm.ncells; c += kBinThreads)
+        for (int w = 0; w < kBinWarps; w++) sm.mask[w * sm.ncells + c] = 0;
+    for (int i = threadIdx.x; i < (sm.ncells + 31) / 32; i += kBinThreads) sm.touched[i] = 0;
+    if (threadIdx.x == 0) *sm.ntouch = 0;
+    __syncthreads();
+}
+
+// Ranked scatter of one round of items into per-cell lists: the rank of an
+// entry in its cell is the number of earlier items (lower warp, then lower
+// lane) of the round that touch the cell, plus the cell's running count.
+// kTrack keeps the list of touched cells so the per-round bookkeeping costs
+// O(touched cells) -- worth it over a bin grid, where a round touches few of
+// up to 1024 bins; over the tiles of one bin most cells are touched and the
+// dense loops are cheaper.
+template <bool kTrack>
 __device__ __forceinline__ void scatterRound(RoundShared& rs, bool valid, const TriGeom& g, U32 entry, const Grid& gr,
-                                             int ncells, U32* s_mask, S32* s_pre, S32* s_run, S32* s_tot, U32* list,
-                                             S64 capacity) {
+                                             const ScatterSmem& sm, U32* list, S64 capacity) {
+    const int n = sm.ncells;
     visitRound(rs, valid, g, entry, gr, true, [&](int cell, S32 who, U32) {
-        atomicOr(&s_mask[(who >> 5) * ncells + cell], 1u << (who & 31));
+        const U32 old = atomicOr(&sm.mask[(who >> 5) * n + cell], 1u << (who & 31));
+        if (kTrack && old == 0u) {
+            const U32 bit = 1u << (cell & 31);
+            if (!(atomicOr(&sm.touched[cell >> 5], bit) & bit)) sm.list[atomicAdd(sm.ntouch, 1)] = (uint16_t)cell;
+        }
     });
     __syncthreads();
-    for (int c = threadIdx.x; c < ncells; c += kBinThreads) {
+    const int nt = kTrack ? *sm.ntouch : n;
+    for (int i = threadIdx.x; i < nt; i += kBinThreads) {
+        const int c = kTrack ? sm.list[i] : i;
         S32 acc = 0;
         for (int w = 0; w < kBinWarps; w++) {
-            s_pre[w * ncells + c] = acc;
-            acc += __popc(s_mask[w * ncells + c]);
+            sm.pre[w * n + c] = acc;
+            acc += __popc(sm.mask[w * n + c]);
         }
-        s_tot[c] = acc;
+        sm.tot[c] = acc;
     }
     __syncthreads();
     visitRound(rs, valid, g, entry, gr, false, [&](int cell, S32 who, U32 e) {
         const int w = who >> 5;
         const U32 lt = (1u << (who & 31)) - 1u;
-        S64 idx = (S64)s_run[cell] + s_pre[w * ncells + cell] + __popc(s_mask[w * ncells + cell] & lt);
+        S64 idx = (S64)sm.run[cell] + sm.pre[w * n + cell] + __popc(sm.mask[w * n + cell] & lt);
         if (idx < capacity) list[idx] = e;
     });
     __syncthreads();
-    for (int c = threadIdx.x; c < ncells; c += kBinThreads) {
-        s_run[c] += s_tot[c];
-        for (int w = 0; w < kBinWarps; w++) s_mask[w * ncells + c] = 0;
+    for (int i = threadIdx.x; i < nt; i += kBinThreads) {
+        const int c = kTrack ? sm.list[i] : i;
+        sm.run[c] += sm.tot[c];
+        for (int w = 0; w < kBinWarps; w++) sm.mask[w * n + c] = 0;
+        if (kTrack) sm.touched[c >> 5] = 0;
     }
     __syncthreads();
+    if (kTrack && threadIdx.x == 0) *sm.ntouch = 0;
 }
 
 // One CTA per chunk: writes the chunk's entries into the bin lists. Within a
@@ -275,7 +390,7 @@ __device__ __forceinline__ void scatterRound(RoundShared& rs, bool valid, const 
 __global__ void __launch_bounds__(kBinThreads, 2) binScatterKernel(DrawDev d) {
     extern __shared__ S32 smem[];
     __shared__ RoundShared rs;
-    __shared__ U32 s_items[kBinThreads * kMaxSubtrisPerTri];
+    __shared__ U32 s_items[kWindow];
     __shared__ S32 s_scratch[kBinWarps + 1];
     __shared__ int s_inst;
     if (__ldg(&d.counters->overflow) & (kOverflowSubtris | kOverflowBin)) return;
@@ -285,35 +400,30 @@ __global__ void __launch_bounds__(kBinThreads, 2) binScatterKernel(DrawDev d) {
     const InstanceDev* in = &d.inst[s_inst];
     const Grid gr = binGrid(in, d.binLog2);
     const int nb = (gr.cx1 + 1) * (gr.cy1 + 1);
-    U32* s_mask = (U32*)smem;                         // [kBinWarps][nb]
-    S32* s_pre = smem + kBinWarps * nb;               // [kBinWarps][nb]
-    S32* s_run = s_pre + kBinWarps * nb;              // [nb]
-    S32* s_tot = s_run + nb;                          // [nb]
+    const ScatterSmem sm = carveScatter(smem, nb);
+    clearScatter(sm);
 
     const int local = chunk - __ldg(&in->chunkBase);
     const S32 binBase = __ldg(&in->binBase);
     const S32* offs = d.chunkBinCount + __ldg(&in->chunkCountBase) + (S64)local * nb;
-    for (int b = threadIdx.x; b < nb; b += kBinThreads) {
-        s_run[b] = __ldg(&d.binStart[binBase + b]) + offs[b];
-        for (int w = 0; w < kBinWarps; w++) s_mask[w * nb + b] = 0;
-    }
+    for (int b = threadIdx.x; b < nb; b += kBinThreads) sm.run[b] = __ldg(&d.binStart[binBase + b]) + offs[b];
     const S64 triBase = __ldg(&in->triBase);
     const S64 t0 = triBase + (S64)local * __ldg(&in->chunkTris);
     const S64 t1 = min(t0 + __ldg(&in->chunkTris), triBase + __ldg(&in->numTris));
     __syncthreads();
-    for (S64 r0 = t0; r0 < t1; r0 += kBinThreads) {
-        ItemRound ir = expandRound(d, r0, t1, s_items, s_scratch);
-        for (S32 k0 = 0; k0 < ir.m; k0 += kBinThreads) {
-            const S32 k = k0 + threadIdx.x;
-            const bool valid = k < ir.m;
-            U32 entry = 0;
-            TriGeom g{};
-            if (valid) {
-                entry = s_items[k];
-                g = geomFromHeader(d.triHeader[entrySlot(entry, d.triHeader)]);
-            }
-            scatterRound(rs, valid, g, entry, gr, nb, s_mask, s_pre, s_run, s_tot, d.binList, d.maxBinEntries);
+    S64 next = t0;
+    for (S32 fill = 0;;) {
+        fill = refillWindow(d, next, t1, fill, s_items, s_scratch);
+        if (fill == 0) break;
+        const bool valid = (S32)threadIdx.x < fill;
+        U32 entry = 0;
+        TriGeom g{};
+        if (valid) {
+            entry = s_items[threadIdx.x];
+            g = geomFromHeader(d.triHeader[entrySlot(entry, d.triHeader)]);
         }
+        scatterRound<true>(rs, valid, g, entry, gr, sm, d.binList, d.maxBinEntries);
+        fill = consumeWindow(s_items, fill);
     }
 }
 
@@ -323,6 +433,15 @@ struct UnitInfo {
     const InstanceDev* in;
     S32 gb, seg, bx, by, e0, e1;
 };
+
+// Next coarse unit for this CTA (dynamic assignment, so CTAs that drew heavy
+// units take fewer). Contains a barrier; the result is uniform.
+__device__ __forceinline__ int nextUnit(S32* counter, int* s_unit) {
+    __syncthreads();
+    if (threadIdx.x == 0) *s_unit = atomicAdd(counter, 1);
+    __syncthreads();
+    return *s_unit;
+}
 
 __device__ __forceinline__ void loadUnit(const DrawDev& d, int u, UnitInfo& ui, int* s_inst) {
     if (threadIdx.x == 0) *s_inst = findInstance(d.binPrefix, d.numInstances, __ldg(&d.unitBin[u]));
@@ -353,15 +472,18 @@ __device__ __forceinline__ Grid tileGrid(const UnitInfo& ui, int binLog2) {
     return gr;
 }
 
-// Persistent CTAs over coarse units: per-unit tile counts.
+// Persistent CTAs over coarse units (taken dynamically): per-unit tile counts.
 __global__ void __launch_bounds__(kBinThreads, 2) coarseCountKernel(DrawDev d) {
     extern __shared__ S32 s_count[];
     __shared__ RoundShared rs;
     __shared__ int s_inst;
     if (__ldg(&d.counters->overflow) & (kOverflowSubtris | kOverflowBin)) return;
+    __shared__ int s_unit;
     const int tpb = 1 << (2 * d.binLog2);
     const S32 numUnits = (S32)min((S64)*(volatile S32*)&d.counters->numUnits, d.maxUnits);
-    for (int u = blockIdx.x; u < numUnits; u += gridDim.x) {
+    for (;;) {
+        const int u = nextUnit(&d.counters->coarseWork[0], &s_unit);
+        if (u >= numUnits) break;
         UnitInfo ui;
         loadUnit(d, u, ui, &s_inst);
         for (int t = threadIdx.x; t < tpb; t += kBinThreads) s_count[t] = 0;
@@ -442,8 +564,9 @@ __global__ void __launch_bounds__(kBinThreads) coarseScanKernel(DrawDev d) {
     }
 }
 
-// Persistent CTAs over coarse units: writes tile list entries, ranked per
-// 512-entry round by per-warp ballot masks over the tiles of the bin.
+// Persistent CTAs over coarse units (taken dynamically): writes tile list
+// entries, ranked per 512-entry round by per-warp ballot masks over the tiles
+// of the bin.
 __global__ void __launch_bounds__(kBinThreads, 2) coarseScatterKernel(DrawDev d) {
     extern __shared__ S32 smem[];
     __shared__ RoundShared rs;
@@ -451,14 +574,13 @@ __global__ void __launch_bounds__(kBinThreads, 2) coarseScatterKernel(DrawDev d)
     if (__ldg(&d.counters->overflow) & (kOverflowSubtris | kOverflowBin | kOverflowTile)) return;
     const int tpb = 1 << (2 * d.binLog2);
     const S32 side = 1 << d.binLog2;
-    U32* s_mask = (U32*)smem;                // [kBinWarps][tpb]
-    S32* s_pre = smem + kBinWarps * tpb;     // [kBinWarps][tpb]
-    S32* s_run = s_pre + kBinWarps * tpb;    // [tpb]
-    S32* s_tot = s_run + tpb;                // [tpb]
+    __shared__ int s_unit;
+    const ScatterSmem sm = carveScatter(smem, tpb);
     const S32 numUnits = (S32)min((S64)*(volatile S32*)&d.counters->numUnits, d.maxUnits);
-    for (int t = threadIdx.x; t < tpb; t += kBinThreads)
-        for (int w = 0; w < kBinWarps; w++) s_mask[w * tpb + t] = 0;
-    for (int u = blockIdx.x; u < numUnits; u += gridDim.x) {
+    clearScatter(sm);
+    for (;;) {
+        const int u = nextUnit(&d.counters->coarseWork[1], &s_unit);
+        if (u >= numUnits) break;
         UnitInfo ui;
         loadUnit(d, u, ui, &s_inst);
         const Grid gr = tileGrid(ui, d.binLog2);
@@ -469,7 +591,7 @@ __global__ void __launch_bounds__(kBinThreads, 2) coarseScatterKernel(DrawDev d)
             S32 v = 0;
             if (tx <= gr.cx1 && ty <= gr.cy1)
                 v = __ldg(&d.tileStart[tileBase + ty * wt + tx]) + __ldg(&d.unitTileCount[(S64)u * tpb + t]);
-            s_run[t] = v;
+            sm.run[t] = v;
         }
         __syncthreads();
         for (S32 e0 = ui.e0; e0 < ui.e1; e0 += kBinThreads) {
@@ -481,20 +603,15 @@ __global__ void __launch_bounds__(kBinThreads, 2) coarseScatterKernel(DrawDev d)
                 entry = __ldg(&d.binList[e]);
                 g = geomFromHeader(d.triHeader[entrySlot(entry, d.triHeader)]);
             }
-            scatterRound(rs, valid, g, entry, gr, tpb, s_mask, s_pre, s_run, s_tot, d.tileList, d.maxTileEntries);
+            scatterRound<false>(rs, valid, g, entry, gr, sm, d.tileList, d.maxTileEntries);
         }
     }
 }
 
 // ------------------------------------------------------------ launchers
 
-size_t binScatterSmem(int maxBins) {
-    return sizeof(S32) * ((size_t)2 * kBinWarps * maxBins + 2 * maxBins);
-}
-size_t coarseScatterSmem(int binLog2) {
-    int tpb = 1 << (2 * binLog2);
-    return sizeof(S32) * ((size_t)2 * kBinWarps * tpb + 2 * tpb);
-}
+size_t binScatterSmem(int maxBins) { return scatterSmemBytes(maxBins); }
+size_t coarseScatterSmem(int binLog2) { return scatterSmemBytes(1 << (2 * binLog2)); }
 
 cudaError_t launchBinning(const DrawDev& d, int maxBins, int numSMs, cudaStream_t stream, cudaEvent_t evCoarse) {
     static bool configured = false;
@@ -511,7 +628,8 @@ cudaError_t launchBinning(const DrawDev& d, int maxBins, int numSMs, cudaStream_
     binScanKernel<<<d.totalBins, kBinThreads, 0, stream>>>(d);
     if (d.totalChunks > 0) binScatterKernel<<<d.totalChunks, kBinThreads, binScatterSmem(maxBins), stream>>>(d);
     if (evCoarse) cudaEventRecord(evCoarse, stream);
-    const int coarseGrid = numSMs * 3;
+    // Persistent coarse CTAs: as many as are resident at once (2 per SM).
+    const int coarseGrid = numSMs * 2;
     coarseCountKernel<<<coarseGrid, kBinThreads, sizeof(S32) * tpb, stream>>>(d);
     coarseScanKernel<<<d.totalBins, kBinThreads, 0, stream>>>(d);
     coarseScatterKernel<<<coarseGrid, kBinThreads, coarseScatterSmem(d.binLog2), stream>>>(d);

@@ -426,9 +426,12 @@ cr_status buildPlan(cr_context* ctx, const std::vector<HostInstance>& in, Plan& 
         d.tileBase = tiles;
         int chunkTris = ctx->tuning.bin_chunk_tris;
         if (chunkTris <= 0) {
-            int64_t want = (int64_t)d.numTris / std::max(1, ctx->numSMs * 4);
-            want = (want + 511) / 512 * 512;
-            chunkTris = (int)std::min<int64_t>(std::max<int64_t>(want, 2048), 65536);
+            // Whole waves of the bin CTAs (2 resident per SM), chunks of at most
+            // 65536 and (for small draws) at least 1024 triangles.
+            const int64_t slots = std::max(1, ctx->numSMs * 2);
+            const int64_t waves = std::max<int64_t>(1, ((int64_t)d.numTris + slots * 65536 - 1) / (slots * 65536));
+            const int64_t want = ((int64_t)d.numTris + slots * waves - 1) / (slots * waves);
+            chunkTris = (int)std::min<int64_t>(std::max<int64_t>(want, 1024), 65536);
         }
         d.chunkTris = chunkTris;
         d.numChunks = (d.numTris + chunkTris - 1) / chunkTris;

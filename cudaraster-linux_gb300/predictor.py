@@ -296,7 +296,8 @@ class QueuePredictor:
 
     def counters_of(self, frame: int) -> np.ndarray:
         """The 8 device counters of a stepped frame (extra subtriangles, bin
-        entries, coarse units, tile entries, fine tiles, overflow flags, -, -)."""
+        entries, coarse units, tile entries, fine tiles, overflow flags, and
+        the two coarse work counters)."""
         return self._host[frame % self.ring][4:].view(np.int32)
 
     # ---------------------------------------------------------------- sizing

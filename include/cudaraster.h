@@ -239,7 +239,8 @@ cr_status cr_get_queue_buffers(cr_context* ctx, const int32_t** bin_counts, cons
 /* Device-to-device copies, ordered on `stream` after the last draw, of its
  * per-bin bin-queue entry counts [num_bins], per-tile tile-queue entry counts
  * [num_tiles] and its 8 device counters (extra subtriangles, bin entries,
- * coarse units, tile entries, fine tiles taken, overflow flags, 2 reserved).
+ * coarse units, tile entries, fine tiles taken, overflow flags, and the two
+ * coarse work counters).
  * Any of the three pointers may be NULL. After an overflow the counts of the
  * overflowing stage and later ones are incomplete. */
 cr_status cr_queue_counts(cr_context* ctx, int32_t* bin_counts, int32_t num_bins, int32_t* tile_counts,

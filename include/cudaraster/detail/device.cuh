@@ -83,7 +83,7 @@ struct Counters {
     S32 tileEntries;          // total tile list entries
     S32 fineTile;             // fine-stage work counter
     S32 overflow;             // kOverflow* bits
-    S32 pad[2];
+    S32 coarseWork[2];        // coarse count / scatter unit counters (dynamic unit assignment)
 };
 
 // Buffers shared by every instance of a draw.
