@@ -38,5 +38,13 @@ public:
 
 template <> struct FragmentShaderTraits<FragmentShader_passthrough> { static constexpr bool mayDiscard = false; };
 template <> struct FragmentShaderTraits<TriHashShader> { static constexpr bool mayDiscard = false; };
+template <> struct FragmentShaderReads<FragmentShader_passthrough> {
+    static constexpr bool center = false;
+    static constexpr bool centroid = false;
+};
+template <> struct FragmentShaderReads<TriHashShader> {
+    static constexpr bool center = false;
+    static constexpr bool centroid = false;
+};
 
 }  // namespace FW

@@ -199,6 +199,18 @@ template <> struct BlendShaderTraits<BlendReplace> { static constexpr bool needs
 template <> struct BlendShaderTraits<BlendDepthOnly> { static constexpr bool needsDst = false; };
 template <class FS> struct FragmentShaderTraits { static constexpr bool mayDiscard = true; };
 template <> struct FragmentShaderTraits<GouraudShader> { static constexpr bool mayDiscard = false; };
+// Which barycentrics a fragment shader reads: the pixel centre's
+// (m_center, m_centerDX, m_centerDY) and the centroid's (m_centroid ...).
+// The fine stage skips computing the ones a shader never reads; with one
+// sample per pixel both are the same values.
+template <class FS> struct FragmentShaderReads {
+    static constexpr bool center = true;
+    static constexpr bool centroid = true;
+};
+template <> struct FragmentShaderReads<GouraudShader> {
+    static constexpr bool center = false;
+    static constexpr bool centroid = true;
+};
 
 // Profiling modes (PixelPipe.hpp:208-213). Only the default mode (per-stage
 // events + device counters) exists here.

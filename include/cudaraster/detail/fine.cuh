@@ -40,6 +40,7 @@ constexpr int kFineMaxThreads = 256;
 // their coverage from their own lane; larger ones from the whole warp.
 constexpr int kFineSelfPixels = 12;
 
+
 template <int S>
 struct FineWarpSmem {
     static constexpr int kTileWords = 64 << S;
@@ -185,13 +186,15 @@ __device__ __forceinline__ U32 shadeFragment(const U32* td, S32 triIdx, S32 X, S
         fs.m_centroidDX = fs.m_centerDX;
         fs.m_centroidDY = fs.m_centerDY;
     } else {
-        computeBarys<S>(fs.m_center, fs.m_centerDX, fs.m_centerDY, td + 4, td + 7, td + 10, (X * 2 + 1) << S,
-                        (Y * 2 + 1) << S);
+        using Reads = FW::FragmentShaderReads<FS>;
+        if (Reads::center || (S == 0 && Reads::centroid))
+            computeBarys<S>(fs.m_center, fs.m_centerDX, fs.m_centerDY, td + 4, td + 7, td + 10, (X * 2 + 1) << S,
+                            (Y * 2 + 1) << S);
         if (S == 0) {
             fs.m_centroid = fs.m_center;
             fs.m_centroidDX = fs.m_centerDX;
             fs.m_centroidDY = fs.m_centerDY;
-        } else {
+        } else if (Reads::centroid) {
             U32 c = centroidCode(S, sampleMask);
             computeBarys<S>(fs.m_centroid, fs.m_centroidDX, fs.m_centroidDY, td + 4, td + 7, td + 10,
                             (X << (S + 1)) + (S32)(c & 0xF), (Y << (S + 1)) + (S32)(c >> 4));
@@ -264,6 +267,10 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
         const S32 stride4 = __ldg(&in->stride4);
         const float4* verts = (const float4*)__ldg((const unsigned long long*)&in->vertices);
 
+        // Visibility keys: depth << 32 | order, order = list position + 1; with
+        // MSAA the low word also carries the winner's coverage mask of the
+        // pixel (order << 8 | mask) while positions fit in 24 bits.
+        const bool packed = S != 0 && count < (1 << 24) - 1;
         if constexpr (kVisibility) {
             for (int w = lane; w < TW; w += 32) sm.key[w] = (U64)sm.depth[w] << 32;
             __syncwarp();
@@ -303,17 +310,18 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
                         self = true;  // no pixel of the tile can be covered
                     } else if ((bx1 - bx0 + 1) * (by1 - by0 + 1) <= kFineSelfPixels) {
                         self = true;
-                        const U64 order = (U64)(U32)(batch + lane + 1);
+                        const U32 order = (U32)(batch + lane + 1);
                         for (S32 py = by0; py <= by1; py++) {
                             for (S32 px = bx0; px <= bx1; px++) {
                                 const U32 X = (U32)(tx * 8 + px), Y = (U32)(ty * 8 + py);
                                 if constexpr (kVisibility) {
                                     const U32 smask = sampleMaskOf<S>(te.E, te.A, te.B, px, py);
+                                    const U64 low = packed ? (order << 8 | smask) : order;
 #pragma unroll
                                     for (int i = 0; i < NS; i++) {
                                         if (!(smask >> i & 1)) continue;
                                         const int idx = py * 8 * NS + i * 8 + px;
-                                        const U64 k = ((U64)sampleDepth<S>(q0.x, q0.y, q0.z, X, Y, i) << 32) | order;
+                                        const U64 k = ((U64)sampleDepth<S>(q0.x, q0.y, q0.z, X, Y, i) << 32) | low;
                                         if (k < sm.key[idx]) atomicMin((unsigned long long*)&sm.key[idx], (unsigned long long)k);
                                     }
                                 } else {
@@ -348,17 +356,18 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
                     const S32 A[3] = {sm.A[0][j], sm.A[1][j], sm.A[2][j]};
                     const S32 B[3] = {sm.B[0][j], sm.B[1][j], sm.B[2][j]};
                     const U32 zx = sm.td[0][j], zy = sm.td[1][j], zb = sm.td[2][j];
-                    const U64 order = (U64)(U32)(batch + j + 1);
+                    const U32 order = (U32)(batch + j + 1);
 #pragma unroll
                     for (int half = 0; half < 2; half++) {
                         const S32 pyy = half ? py1 : py0;
                         const U32 Y = half ? pY1 : pY0;
                         const U32 smask = sampleMaskOf<S>(E, A, B, px, pyy);
+                        const U64 low = packed ? (order << 8 | smask) : order;
 #pragma unroll
                         for (int i = 0; i < NS; i++) {
                             if (!(smask >> i & 1)) continue;
                             const int idx = pyy * 8 * NS + i * 8 + px;
-                            const U64 k = ((U64)sampleDepth<S>(zx, zy, zb, pX, Y, i) << 32) | order;
+                            const U64 k = ((U64)sampleDepth<S>(zx, zy, zb, pX, Y, i) << 32) | low;
                             if (k < sm.key[idx]) sm.key[idx] = k;
                         }
                     }
@@ -530,45 +539,65 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
         }
 
         if constexpr (kVisibility) {
-            // ---- Resolve: shade every (pixel, winning triangle) once.
-            for (int p = lane; p < 64; p += 32) {
-                const S32 px = p & 7, py = p >> 3;
-                const int rowBase = py * 8 * NS + px;
-                U32 done = 0;
-                for (int i0 = 0; i0 < NS; i0++) {
-                    if (done >> i0 & 1) continue;
-                    const U64 k0 = sm.key[rowBase + i0 * 8];
-                    const U32 order = (U32)k0;
-                    if (order == 0) continue;  // no fragment passed the depth test here
-                    // Samples won by the same fragment.
-                    U32 won = 0;
+            // ---- Resolve: shade every (pixel, winning triangle) once. A lane
+            // owns pixels lane and lane + 32; sample i0 of a pixel starts a
+            // winner if no earlier sample of the pixel has the same key low
+            // word (with MSAA the low word carries the winner's coverage mask,
+            // so neither its edges nor its mask are recomputed here).
+#pragma unroll 1
+            for (int i0 = 0; i0 < NS; i0++) {
+                U32 low[2], won[2], tri[2], td[2][16];
+                auto fetch = [&](int h) {
+                    const int p = lane + 32 * h;
+                    const int rowBase = (p >> 3) * 8 * NS + (p & 7);
+                    low[h] = (U32)sm.key[rowBase + i0 * 8];
+                    won[h] = 0;
+                    if (low[h] != 0) {
+                        bool first = true;
+                        for (int i = 0; i < i0; i++)
+                            if ((U32)sm.key[rowBase + i * 8] == low[h]) first = false;
+                        if (first)
 #pragma unroll
-                    for (int i = 0; i < NS; i++)
-                        if ((U32)sm.key[rowBase + i * 8] == order) won |= 1u << i;
-                    done |= won;
-                    const U32 entry = __ldg(&d.tileList[start + (S32)order - 1]);
-                    const U32 tri = entry >> 3, sub = entry & 7;
-                    const S64 slot = (sub == 7) ? (S64)tri : (S64)__ldg(&d.triHeader[tri].w) + sub;
-                    U32 smask = 1;
-                    if (S != 0) {
-                        const TileEdges te = tileEdges(__ldg(&d.triHeader[slot]), cx0, cy0);
-                        smask = sampleMaskOf<S>(te.E, te.A, te.B, px, py);
+                            for (int i = 0; i < NS; i++)
+                                if ((U32)sm.key[rowBase + i * 8] == low[h]) won[h] |= 1u << i;
                     }
-                    const uint4* tdp = &d.triData[slot * 4];
-                    uint4 q0 = __ldg(&tdp[0]), q1 = __ldg(&tdp[1]), q2 = __ldg(&tdp[2]), q3 = __ldg(&tdp[3]);
-                    const U32 td[16] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w,
-                                        q2.x, q2.y, q2.z, q2.w, q3.x, q3.y, q3.z, q3.w};
+                    tri[h] = 0;
+                    if (won[h]) {
+                        const U32 entry = __ldg(&d.tileList[start + (S32)(packed ? (low[h] >> 8) : low[h]) - 1]);
+                        const U32 sub = entry & 7;
+                        tri[h] = entry >> 3;
+                        const S64 slot = (sub == 7) ? (S64)tri[h] : (S64)__ldg(&d.triHeader[tri[h]].w) + sub;
+                        const uint4* tdp = &d.triData[slot * 4];
+                        const uint4 q1 = __ldg(&tdp[1]), q2 = __ldg(&tdp[2]), q3 = __ldg(&tdp[3]);
+                        td[h][4] = q1.x; td[h][5] = q1.y; td[h][6] = q1.z; td[h][7] = q1.w;
+                        td[h][8] = q2.x; td[h][9] = q2.y; td[h][10] = q2.z; td[h][11] = q2.w;
+                        td[h][12] = q3.x; td[h][13] = q3.y; td[h][14] = q3.z; td[h][15] = q3.w;
+                        if (S != 0 && !packed) {
+                            const TileEdges te = tileEdges(__ldg(&d.triHeader[slot]), cx0, cy0);
+                            low[h] = sampleMaskOf<S>(te.E, te.A, te.B, p & 7, p >> 3);
+                        } else if (S != 0) {
+                            low[h] &= 0xFFu;
+                        }
+                    }
+                };
+                auto shade = [&](int h) {
+                    if (!won[h]) return;
+                    const int p = lane + 32 * h;
+                    const S32 px = p & 7, py = p >> 3;
+                    const int rowBase = py * 8 * NS + px;
                     bool discard;
                     const S32 X = tx * 8 + px, Y = ty * 8 + py;
-                    const U32 src = shadeFragment<FS, S, F>(td, (S32)((S64)tri - triBase), X, Y, smask, verts, stride4,
+                    const S32 triIdx = (S32)((S64)tri[h] - triBase);
+                    // low[h] now holds the winner's coverage mask of the pixel (MSAA).
+                    const U32 src = shadeFragment<FS, S, F>(td[h], triIdx, X, Y, S != 0 ? low[h] : 1u, verts, stride4,
                                                             sm.shared, 0u, discard);
                     BS bs;
 #pragma unroll
                     for (int i = 0; i < NS; i++) {
-                        if (!(won >> i & 1)) continue;
+                        if (!(won[h] >> i & 1)) continue;
                         const int idx = rowBase + i * 8;
                         sm.depth[idx] = (U32)(sm.key[idx] >> 32);
-                        bs.m_triIdx = (S32)((S64)tri - triBase);
+                        bs.m_triIdx = triIdx;
                         bs.m_pixelPos = FW::Vec2i(X, Y);
                         bs.m_sampleIdx = i;
                         bs.m_src = src;
@@ -578,7 +607,13 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
                         bs.run();
                         if (bs.m_writeColor) sm.color[idx] = bs.m_color;
                     }
-                }
+                };
+                // One pixel at a time: fetching both pixels' data before
+                // shading either measured slower (registers, occupancy).
+                fetch(0);
+                shade(0);
+                fetch(1);
+                shade(1);
             }
             __syncwarp();
         }
