@@ -231,6 +231,10 @@ def main():
     ap.add_argument("--no-subpixel", action="store_true", help="skip the 4x MSAA grazing-heightfield frame")
     ap.add_argument("--profile-frames", type=int, default=0,
                     help="only draw this many frames of the workload (for ncu captures), print nothing else")
+    ap.add_argument("--profile-workload", default="soup1m", choices=["soup1m", "subpixel", "flythrough", "flythrough2048",
+                                                              "predicted"],
+                    help="workload of --profile-frames: the 1M soup (default), the 4x MSAA heightfield, plain "
+                         "fly-through frames, or predictor-sized fly-through frames (12 of them, 8 training)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
@@ -250,6 +254,9 @@ def main():
 
     workloads = importlib.import_module(PKG + ".workloads")
     tuning = workloads.load_tuning("soup1m")
+    if args.profile_frames > 0 and args.profile_workload != "soup1m":
+        print(json.dumps(workloads.profile_frames(args.profile_workload, args.profile_frames, tuning)))
+        return
     cr = pkg.CudaRaster()
     cr.init()
     if tuning:

@@ -27,7 +27,8 @@
 
 #include "cudaraster.h"
 
-namespace {
+namespace cr {
+namespace predictor {
 
 constexpr int kTile = 32;          // GEMM output tile (rows x cols) and k-slab
 constexpr int kGemmThreads = 256;  // 32 columns x 8 row groups, 4 rows per thread
@@ -415,7 +416,10 @@ __global__ void __launch_bounds__(1024) predictorFrameKernel(FrameArgs a, const 
     if (threadIdx.x < 8) reinterpret_cast<int32_t*>(a.fetch + 4)[threadIdx.x] = a.counters ? a.counters[threadIdx.x] : 0;
 }
 
-}  // namespace
+}  // namespace predictor
+}  // namespace cr
+
+using namespace cr::predictor;
 
 // ---------------------------------------------------------------- the network
 struct cr_predictor {

@@ -490,3 +490,22 @@ def measure_subpixel(n: int = 2048, width: int = 3840, height: int = 2160, sampl
                "counters": {k: c[k] for k in ("num_subtris", "bin_entries", "tile_entries", "coarse_units",
                                               "reruns", "overflow")}}
     return summary, (color.tensor.clone(), depth.tensor.clone()), sc
+
+
+def profile_frames(name: str, frames: int, tuning: dict | None = None) -> dict:
+    """Draws a few frames of a workload and nothing else (for profiler runs):
+    "subpixel" (the 4x MSAA heightfield), "flythrough" / "flythrough2048"
+    (plain fly-through frames 100..100+frames over the 4096^2 or a 2048^2
+    heightfield) or "predicted" (a short predictor-sized
+    fly-through: `frames` frames, the first two thirds plain and training)."""
+    if name == "subpixel":
+        s, _, _ = measure_subpixel(steps=frames, warmup=0, tuning=tuning)
+        return {"profile": name, "frames": frames, "counters": s["counters"]}
+    ft = FlyThrough(n=2048 if name == "flythrough2048" else 4096, frames=max(frames, 3) + 100)
+    if name in ("flythrough", "flythrough2048"):
+        run_flythrough_plain(ft, range(100, 100 + frames), tuning)
+        return {"profile": name, "frames": frames, "tris": ft.num_tris}
+    if name == "predicted":
+        res = run_flythrough_predicted(ft, frames, max(3, (2 * frames) // 3), tuning)
+        return {"profile": name, "frames": frames, "misses": res["misses"], "adam_steps": res["adam_steps"]}
+    raise ValueError(name)
