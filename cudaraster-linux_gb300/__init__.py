@@ -7,4 +7,4 @@ directory name contains a hyphen, so import it with
 importlib.import_module("cudaraster-linux_gb300").
 """
 from .raster import (Buffer, CudaRaster, CudaSurface, DebugParams, RasterError, Stats, clear_depth_from_float,  # noqa: F401
-                     color_to_abgr, encode_depth, pipe_info, pipe_names)
+                     color_to_abgr, encode_depth, pipe_info, pipe_names, write_ppm)

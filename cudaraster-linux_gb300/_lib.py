@@ -94,6 +94,7 @@ _SIGNATURES = {
                                            C.c_void_p, C.c_char_p, C.c_int64]),
     "cr_vertex_shader_passthrough": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
                                                C.c_int64, C.POINTER(C.c_float), C.c_void_p]),
+    "cr_resolve_color": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p]),
     "cr_get_queue_layout": (C.c_int, [C.c_void_p, C.POINTER(QueueLayout)]),
     "cr_queue_counts": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     "cr_queue_features": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_float), C.c_void_p, C.c_void_p]),

@@ -91,6 +91,18 @@ class CudaSurface:
         """Raw words (uint32 values in an int64 tensor), shape (rows, rowWords)."""
         return self.tensor.cpu().to(torch.int64) & 0xFFFFFFFF
 
+    def resolve(self, stream: torch.cuda.Stream | None = None) -> torch.Tensor:
+        """MSAA resolve of a colour surface (cr_resolve_color): a (height,
+        width, 4) uint8 tensor on the device, channels R, G, B, A."""
+        if self.getFormat() != self.FORMAT_RGBA8:
+            raise RasterError(1, "CudaSurface: only colour surfaces resolve")
+        w, h = self.getSize()
+        out = torch.empty((h, w, 4), dtype=torch.uint8, device=self.tensor.device)
+        s = (stream or torch.cuda.current_stream()).cuda_stream
+        check(_lib.load().cr_resolve_color(self.getDevicePtr(), w, h, self.getNumSamples(), out.data_ptr(), w * 4,
+                                           C.c_void_p(s)))
+        return out
+
     def fill(self, value: int) -> None:
         v = value - (1 << 32) if value >= (1 << 31) else value
         self.tensor.fill_(v)
@@ -383,3 +395,15 @@ def color_to_abgr(r, g, b, a) -> int:
 
 def clear_depth_from_float(d: float) -> int:
     return _lib.load().cr_clear_depth_from_float(d)
+
+
+def write_ppm(path, rgba) -> None:
+    """Writes an (height, width, 4) uint8 image (e.g. CudaSurface.resolve())
+    as a binary PPM (alpha dropped), for looking at frames and diffs."""
+    import numpy as np
+    a = rgba.cpu().numpy() if hasattr(rgba, "cpu") else np.asarray(rgba)
+    a = np.ascontiguousarray(a[..., :3], dtype=np.uint8)
+    h, w = a.shape[:2]
+    with open(path, "wb") as f:
+        f.write(b"P6\n%d %d\n255\n" % (w, h))
+        f.write(a.tobytes())

@@ -217,6 +217,17 @@ cr_status cr_vertex_shader_passthrough(const float* model, int32_t model_stride,
                                        int32_t color_stride, void* out_vertices, int32_t out_stride_bytes,
                                        int64_t num_vertices, const float* mvp_row_major, void* stream);
 
+/* ---- MSAA resolve ----
+ * The reference's CudaSurface::resolveToScreen (CudaSurface.hpp:73) is
+ * commented out and drew through GL. This averages each pixel's samples per
+ * channel, rounding half up ((sum + S/2) >> log2 S), into a row-major image of
+ * one RGBA8 word per pixel (R in the low byte); with one sample it copies the
+ * pixels without the 8x8 tile padding. color: a colour surface of width x
+ * height with num_samples samples (device); out: device, out_row_bytes per row
+ * (>= 4 * width, multiple of 4). Asynchronous on stream. */
+cr_status cr_resolve_color(const void* color, int32_t width, int32_t height, int32_t num_samples, void* out,
+                           int64_t out_row_bytes, void* stream);
+
 /* ---- Queue occupancy and the learned queue predictor ----
  * No reference counterpart: the reference sizes its queues from the previous
  * draw and grows them on overflow (CudaRaster.cpp:263-275, 325-342), which

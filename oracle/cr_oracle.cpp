@@ -610,6 +610,21 @@ U32 shade(const ShadeCtx& c, const Data& d, S32 triIdx, S32 px, S32 py, U32 cent
     }
 }
 
+// The test pipe's derivative shader in quad mode (its GPU twin reads the
+// interpolated v barycentric u = m_center.y): colour = (|dFdx u| * 64,
+// |dFdy u| * 64, m_center.z, 1), the differences taken across the 2x2 quad
+// of pixel (x, y) between pixel-centre barycentrics.
+U32 shade_deriv_quad(const ShadeCtx& c, const Data& d, S32 x, S32 y) {
+    const S32 w[3] = {(S32)d.w[4], (S32)d.w[5], (S32)d.w[6]};
+    const S32 u[3] = {(S32)d.w[7], (S32)d.w[8], (S32)d.w[9]};
+    const S32 v[3] = {(S32)d.w[10], (S32)d.w[11], (S32)d.w[12]};
+    auto bary = [&](S32 qx, S32 qy) { return compute_barys(c.s, w, u, v, (qx * 2 + 1) << c.s, (qy * 2 + 1) << c.s); };
+    const S32 x0 = x & ~1, y0 = y & ~1;
+    const F32 dx = bary(x0 + 1, y).c[1] - bary(x0, y).c[1];
+    const F32 dy = bary(x, y0 + 1).c[1] - bary(x, y0).c[1];
+    return to_abgr(std::fabs(dx) * 64.0f, std::fabs(dy) * 64.0f, bary(x, y).c[2], 1.0f);
+}
+
 inline S64 row_words(const or_pipe* p) {
     S64 rw = ((S64)p->width + 7) & ~7LL;
     return rw << p->samples_log2;
@@ -745,8 +760,23 @@ int or_render(const or_pipe* p, const float* vertices, const int32_t* indices,
                     const Subtri& st = res[(size_t)it.tri].sub[it.sub];
                     TriGeom g = geom_from_header(st.h);
                     const U32 zmin = st.h.w[3] & 0xFFFFF000u;
-                    for (int py = 0; py < 8; py++) {
-                        for (int px = 0; px < 8; px++) {
+                    // Quad mode (FineRaster.inl:401-427): a 2x2 quad is shaded when
+                    // any of its pixels is covered; its uncovered pixels are helpers
+                    // that only feed the derivatives (PixelPipe.hpp:62-69: dFdx is
+                    // the right minus the left pixel of the row, dFdy the bottom
+                    // minus the top pixel of the column).
+                    const bool quads = (p->render_mode & OR_QUADS) != 0;
+                    for (int pi = 0; pi < 64; pi++) {
+                        int px, py;
+                        if (quads) {
+                            const int q = pi >> 2, k = pi & 3;
+                            px = ((q & 3) << 1) + (k & 1);
+                            py = ((q >> 2) << 1) + (k >> 1);
+                        } else {
+                            px = pi & 7;
+                            py = pi >> 3;
+                        }
+                        {
                             S32 x = tx * 8 + px, y = ty * 8 + py;
                             U32 mask = sample_mask(vp, s, g, x, y);
                             if (mask == 0) continue;
@@ -768,7 +798,12 @@ int or_render(const or_pipe* p, const float* vertices, const int32_t* indices,
                             }
                             if (!anyPass) continue;
                             bool discard;
-                            U32 src = shade(sc, st.d, (S32)it.tri, x, y, centroid_code(s, mask), &discard);
+                            U32 src;
+                            if (quads && p->shader == OR_SHADER_DERIV)
+                                src = shade_deriv_quad(sc, st.d, x, y);
+                            else
+                                src = shade(sc, st.d, (S32)it.tri, x, y, centroid_code(s, mask), &discard);
+                            discard = quads && p->shader == OR_SHADER_DERIV ? false : discard;
                             if (discard) continue;
                             for (int i = 0; i < ns; i++) {
                                 if (!(mask >> i & 1)) continue;

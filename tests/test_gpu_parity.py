@@ -34,6 +34,26 @@ def test_soup_pipes(cuda, pipe):
     assert_same(gc, gd, rc, rd, pipe)
 
 
+@pytest.mark.parametrize("median_px,seed", [(3.0, 12), (9.0, 13), (40.0, 14)])
+def test_quad_derivatives(cuda, median_px, seed):
+    # Quad mode: derivatives across each 2x2 quad, helper pixels shaded but not written.
+    sc = pkg_mod("scenes").soup(6000, 256, 184, seed=seed, median_px=median_px)
+    clear = clear_of()
+    gc, gd, _, _ = gpu_render("PixelPipe_deriv_quads", sc, clear)
+    rc, rd, st = oracle_render("PixelPipe_deriv_quads", sc, clear)
+    assert st["zmin_violations"] == 0
+    assert_same(gc, gd, rc, rd, "deriv quads")
+    assert len(np.unique(rc)) > 100   # the derivatives vary across the frame
+
+
+def test_quad_derivatives_cube(cuda):
+    sc = pkg_mod("scenes").cube(640, 480)
+    clear = clear_of()
+    gc, gd, _, _ = gpu_render("PixelPipe_deriv_quads", sc, clear)
+    rc, rd, _ = oracle_render("PixelPipe_deriv_quads", sc, clear)
+    assert_same(gc, gd, rc, rd, "deriv quads cube")
+
+
 @pytest.mark.parametrize("pipe", list(PIPE_SAMPLES))
 def test_soup_msaa(cuda, pipe):
     sc = pkg_mod("scenes").soup(8000, 200, 136, seed=5, median_px=5.0)
