@@ -111,7 +111,9 @@ struct cr_context {
     bool userCapacity = false;  // capacities set by cr_set_capacity replace the estimates
     // Device memory.
     DevBuf triSubtris, triHeader, triData, chunkBinCount, binCount, binStart, binUnitFirst, binList;
-    DevBuf unitBin, unitSeg, unitTileCount, tileCount, tileStart, tileList, instBuf, prefixBuf, counters, fineCounters;
+    DevBuf unitBin, unitSeg, unitTileCount, tileCount, tileStart, tileList;
+    DevBuf instBuf;   // instance descriptors, then the prefix arrays (one copy per draw)
+    DevBuf counters;  // Counters, then one fine-stage tile counter per pipe group (one memset per draw)
     // Pinned staging.
     // Descriptor staging for asynchronous draws: a ring of pinned slots, each
     // reused only after the copy that read it has run (stageDone), so a host
@@ -248,7 +250,7 @@ cr_status cr_destroy(cr_context* ctx) {
     DevBuf* bufs[] = {&ctx->triSubtris, &ctx->triHeader, &ctx->triData, &ctx->chunkBinCount, &ctx->binCount,
                       &ctx->binStart, &ctx->binUnitFirst, &ctx->binList, &ctx->unitBin, &ctx->unitSeg,
                       &ctx->unitTileCount, &ctx->tileCount, &ctx->tileStart, &ctx->tileList, &ctx->instBuf,
-                      &ctx->prefixBuf, &ctx->counters, &ctx->fineCounters};
+                      &ctx->counters};
     for (DevBuf* b : bufs) b->release();
     for (int i = 0; i < cr_context::kStageSlots; i++) {
         if (ctx->hostStage[i]) cudaFreeHost(ctx->hostStage[i]);
@@ -508,12 +510,11 @@ cr_status ensureCapacity(cr_context* ctx, const Plan& plan) {
     CR_CUDA(ctx->tileCount.ensure((size_t)plan.totalTiles * 4), "cudaMalloc");
     CR_CUDA(ctx->tileStart.ensure((size_t)plan.totalTiles * 4), "cudaMalloc");
     CR_CUDA(ctx->tileList.ensure((size_t)ctx->maxTileEntries * 4), "cudaMalloc");
-    CR_CUDA(ctx->counters.ensure(sizeof(Counters)), "cudaMalloc");
-    CR_CUDA(ctx->fineCounters.ensure(sizeof(int32_t) * std::max<size_t>(plan.groups.size(), 1)), "cudaMalloc");
+    CR_CUDA(ctx->counters.ensure(sizeof(Counters) + sizeof(int32_t) * std::max<size_t>(plan.groups.size(), 1)),
+            "cudaMalloc");
     size_t instBytes = sizeof(InstanceDev) * plan.inst.size();
     size_t prefBytes = 4 * 3 * (plan.inst.size() + 1) + 8 * (plan.inst.size() + 1) + 64;
-    CR_CUDA(ctx->instBuf.ensure(instBytes), "cudaMalloc");
-    CR_CUDA(ctx->prefixBuf.ensure(prefBytes), "cudaMalloc");
+    CR_CUDA(ctx->instBuf.ensure(instBytes + prefBytes), "cudaMalloc");
     size_t stage = instBytes + prefBytes;
     if (stage > ctx->hostStageBytes) {
         for (int i = 0; i < cr_context::kStageSlots; i++) {
@@ -561,16 +562,18 @@ DrawDev makeDrawDev(cr_context* ctx, const Plan& plan) {
     d.tileStart = ctx->tileStart.as<int32_t>();
     d.tileList = ctx->tileList.as<uint32_t>();
     d.maxTileEntries = ctx->maxTileEntries;
-    char* pref = ctx->prefixBuf.as<char>();
+    char* pref = ctx->instBuf.as<char>() + sizeof(InstanceDev) * plan.inst.size();
     size_t n1 = plan.inst.size() + 1;
     d.triPrefix = (const int64_t*)pref;
     d.chunkPrefix = (const int32_t*)(pref + 8 * n1);
     d.binPrefix = d.chunkPrefix + n1;
     d.tilePrefix = d.binPrefix + n1;
     d.counters = ctx->counters.as<Counters>();
-    d.fineTileCounter = ctx->fineCounters.as<int32_t>();
+    d.fineTileCounter = (int32_t*)(ctx->counters.as<char>() + sizeof(Counters));
     return d;
 }
+
+static_assert(sizeof(InstanceDev) % 8 == 0, "the prefix arrays follow the descriptors with 8-byte alignment");
 
 // Enqueues one draw of `plan` on `stream`. `stage` is pinned host memory for
 // the descriptors (the copy node reads it when a captured graph replays) and
@@ -589,10 +592,10 @@ cr_status launchDrawWith(cr_context* ctx, const Plan& plan, cudaStream_t stream,
     memcpy(hp + 8 * n1, plan.chunkPrefix.data(), 4 * n1);
     memcpy(hp + 12 * n1, plan.binPrefix.data(), 4 * n1);
     memcpy(hp + 16 * n1, plan.tilePrefix.data(), 4 * n1);
-    CR_CUDA(cudaMemcpyAsync(ctx->instBuf.ptr, hs, instBytes, cudaMemcpyHostToDevice, stream), "cudaMemcpyAsync");
-    CR_CUDA(cudaMemcpyAsync(ctx->prefixBuf.ptr, hp, 20 * n1, cudaMemcpyHostToDevice, stream), "cudaMemcpyAsync");
-    CR_CUDA(cudaMemsetAsync(ctx->counters.ptr, 0, sizeof(Counters), stream), "cudaMemsetAsync");
-    CR_CUDA(cudaMemsetAsync(ctx->fineCounters.ptr, 0, sizeof(int32_t) * plan.groups.size(), stream), "cudaMemsetAsync");
+    CR_CUDA(cudaMemcpyAsync(ctx->instBuf.ptr, hs, instBytes + 20 * n1, cudaMemcpyHostToDevice, stream),
+            "cudaMemcpyAsync");
+    CR_CUDA(cudaMemsetAsync(ctx->counters.ptr, 0, sizeof(Counters) + sizeof(int32_t) * plan.groups.size(), stream),
+            "cudaMemsetAsync");
 
     if (events) CR_CUDA(cudaEventRecord(ctx->ev[0], stream), "cudaEventRecord");
     for (const Plan::Group& g : plan.groups)
