@@ -172,10 +172,15 @@ __device__ __noinline__ void setupClipped(const DrawDev& d, S64 gt, int3 vidx, f
     }
 }
 
+// Resident setup CTAs per SM the compiler must allow (register budget).
+#ifndef CR_SETUP_MIN_BLOCKS
+#define CR_SETUP_MIN_BLOCKS 5
+#endif
+
 // triangleSetupImpl (TriangleSetup.inl:219-417), over the triangle range of
 // one pipe group [triBegin, triEnd) (global triangle slots).
 template <int S, U32 F>
-__global__ void __launch_bounds__(256, 4) setupKernel(DrawDev d, int instBegin, int instEnd, S64 triBegin, S64 triEnd) {
+__global__ void __launch_bounds__(256, CR_SETUP_MIN_BLOCKS) setupKernel(DrawDev d, int instBegin, int instEnd, S64 triBegin, S64 triEnd) {
     S64 gt = triBegin + (S64)blockIdx.x * 256 + threadIdx.x;
     if (gt >= triEnd) return;
     int ii = instBegin + findInstance64(d.triPrefix + instBegin, instEnd - instBegin, gt);
