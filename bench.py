@@ -7,7 +7,9 @@ reference's plain path: setup -> bin -> coarse -> fine, then the host reads
 the overflow counters). `value` is device-timed with CUDA events on the
 drawing stream, inputs resident in HBM, L2 flushed (256 MiB write) before
 every step. `e2e` times the same draw with the inputs copied from pinned host
-memory and the framebuffer copied back inside the timed region.
+memory and the framebuffer copied back inside the timed region (wall clock over
+all steps; the next step's inputs upload and the previous step's framebuffer
+downloads on their own streams while the current step draws).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -70,24 +72,29 @@ def stage_traffic(stage: str):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons, sampled every 20 ms from before
+    the timed region starts; mark() brackets the timed region and summary()
+    keeps the samples nvidia-smi timestamped inside it."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index: int):
+    def __init__(self, gpu_index: int, interval_ms: int = 20):
         self.gpu = gpu_index
+        self.interval = interval_ms
         self.proc = None
         self.lines: list[str] = []
+        self.window = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", str(self.interval)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            time.sleep(0.3)  # let the first samples arrive
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
@@ -96,8 +103,12 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
+    def mark(self, start: float, end: float) -> None:
+        self.window = (start, end)
+
     def __exit__(self, *exc):
         if self.proc:
+            time.sleep(2 * self.interval / 1000.0)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -105,22 +116,30 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
-        sm, mx, reasons = [], 0.0, set()
+        import datetime
+        sm, mx, reasons, kept = [], 0.0, set(), 0
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
-            if len(parts) < 9:
+            if len(parts) < 10:
                 continue
             try:
-                sm.append(float(parts[1]))
-                mx = max(mx, float(parts[2]))
+                ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
             except ValueError:
                 continue
-            for n, v in zip(names, parts[5:9]):
+            if self.window and not (self.window[0] - 0.01 <= ts <= self.window[1] + 0.01):
+                continue
+            try:
+                sm.append(float(parts[2]))
+                mx = max(mx, float(parts[3]))
+            except ValueError:
+                continue
+            kept += 1
+            for n, v in zip(names, parts[6:10]):
                 if v.lower().startswith("active"):
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": kept, "interval_ms": self.interval}
 
 
 def cpu_baseline(sc, budget_s: float = 12.0, min_frames: int = 1):
@@ -222,7 +241,7 @@ def subpixel_oracle_check(sc, got):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -295,6 +314,7 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
+        t_start = time.time()
         for i in range(args.steps):
             flush.fill_(i & 0xFF)
             starts[i].record(stream)
@@ -303,6 +323,7 @@ def main():
             s = cr.getStats()
             stage += [s.setupTime, s.binTime, s.coarseTime, s.fineTime]
         torch.cuda.synchronize()
+        clk.mark(t_start, time.time())
     if world > 1:
         dist.barrier()
     step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
@@ -313,41 +334,61 @@ def main():
     stage_ms = stage / args.steps * 1e3
     counters = cr.getCounters()
 
-    # ---- end-to-end through the C ABI with host buffers
+    # ---- end-to-end through the C ABI with host buffers: every step copies its
+    # vertex and index buffers in from pinned host memory and its framebuffer
+    # out. Three input sets (uploaded two steps ahead on a copy stream, so the
+    # link always has a copy queued) and two framebuffers (the previous step's
+    # downloads on a readback stream) rotate while step i draws.
     hv = torch.from_numpy(sc["vertices"]).pin_memory()
     hi = torch.from_numpy(sc["indices"]).pin_memory()
-    hc = torch.empty_like(color.tensor, device="cpu").pin_memory()
-    hd = torch.empty_like(depth.tensor, device="cpu").pin_memory()
-    dv = torch.empty_like(verts)
-    di = torch.empty_like(idx)
-    cr.setVertexBuffer(dv, 0)
-    cr.setIndexBuffer(di, 0, T)
+    hc = [torch.empty_like(color.tensor, device="cpu").pin_memory() for _ in range(2)]
+    hd = [torch.empty_like(depth.tensor, device="cpu").pin_memory() for _ in range(2)]
+    NIN = 3
+    dev_in = [(torch.empty_like(verts), torch.empty_like(idx)) for _ in range(NIN)]
+    fbs = [(color, depth), (pkg.CudaSurface((W, H), pkg.CudaSurface.FORMAT_RGBA8, 1),
+                            pkg.CudaSurface((W, H), pkg.CudaSurface.FORMAT_DEPTH32, 1))]
+    up_stream, down_stream = torch.cuda.Stream(), torch.cuda.Stream()
+    copied = [torch.cuda.Event() for _ in range(NIN)]
+    drawn = [torch.cuda.Event() for _ in range(NIN)]
+    read = [torch.cuda.Event() for _ in range(2)]
 
-    def e2e_step():
-        dv.copy_(hv, non_blocking=True)
-        di.copy_(hi, non_blocking=True)
-        draw()
-        hc.copy_(color.tensor, non_blocking=True)
-        hd.copy_(depth.tensor, non_blocking=True)
+    def upload(k):
+        up_stream.wait_event(drawn[k % NIN])       # the draw that read this input set is done
+        with torch.cuda.stream(up_stream):
+            dev_in[k % NIN][0].copy_(hv, non_blocking=True)
+            dev_in[k % NIN][1].copy_(hi, non_blocking=True)
+        copied[k % NIN].record(up_stream)
 
-    for _ in range(2):
-        e2e_step()
-    torch.cuda.synchronize()
-    e2e_ms = []
-    for i in range(args.steps):
-        flush.fill_(i & 0xFF)
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        e2e_step()
-        b.record(stream)
+    def e2e_run(n):
+        for k in range(min(NIN - 1, n)):
+            upload(k)
+        for k in range(n):
+            if k + NIN - 1 < n:
+                upload(k + NIN - 1)
+            stream.wait_event(copied[k % NIN])
+            stream.wait_event(read[k % 2])          # this framebuffer's previous readback is done
+            dv, di = dev_in[k % NIN]
+            cr.setSurfaces(*fbs[k % 2])
+            cr.setVertexBuffer(dv, 0)
+            cr.setIndexBuffer(di, 0, T)
+            draw()
+            drawn[k % NIN].record(stream)
+            down_stream.wait_event(drawn[k % NIN])
+            with torch.cuda.stream(down_stream):
+                hc[k % 2].copy_(fbs[k % 2][0].tensor, non_blocking=True)
+                hd[k % 2].copy_(fbs[k % 2][1].tensor, non_blocking=True)
+            read[k % 2].record(down_stream)
         torch.cuda.synchronize()
-        e2e_ms.append(a.elapsed_time(b))
-    e2e_total = sum(e2e_ms)
+
+    e2e_run(3)
+    t0 = time.perf_counter()
+    e2e_run(args.steps)
+    e2e_total = (time.perf_counter() - t0) * 1e3
     e2e_total = reduce_max(e2e_total, world, "cuda")
     e2e_value = replica_throughput(world, args.steps, e2e_total)
+    cr.setSurfaces(color, depth)
     h2d = hv.numel() * 4 + hi.numel() * 4
-    d2h = (hc.numel() + hd.numel()) * 4
+    d2h = (hc[0].numel() + hd[0].numel()) * 4
 
     # ---- roofline of the dominant stage (stage events bracket its kernels)
     peak, peak_kind = peaks()
