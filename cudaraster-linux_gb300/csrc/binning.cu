@@ -10,11 +10,12 @@
 //           order and allocates each bin's contiguous list, binScatter writes
 //           the entries ranked inside each 512-item round by per-warp ballot
 //           masks. Every bin list comes out in submission order, with no merge.
-//   coarse: units of consecutive bin-list entries of one bin, with the same
-//           three passes over the tiles of the bin.
+//   coarse: units of consecutive bin-list entries of one bin (sized on the
+//           device once the bin lists are known), each taken by one warp,
+//           with the same three passes over the tiles of the bin.
 //
-// In every round, an item whose bounding box spans more than kSmallCells
-// cells is dealt to a warp (one cell per lane) instead of being walked by its
+// In every bin round, an item whose bounding box spans more than kSmallCells
+// bins is dealt to a warp (one bin per lane) instead of being walked by its
 // own thread, so a few huge triangles do not serialise a round.
 //
 // List entries are triangle << 3 | subtriangle (7 = the triangle's own slot),
@@ -249,12 +250,40 @@ __global__ void __launch_bounds__(kBinThreads, 2) binCountKernel(DrawDev d) {
     for (int b = threadIdx.x; b < nb; b += kBinThreads) out[b] = s_count[b];
 }
 
-// One CTA per global bin: chunk-order exclusive offsets, list allocation and
-// coarse work units.
+// Run by the last bin-scan CTA to finish, once every bin's entry count is
+// known: the coarse unit size (the caller's, or the smallest power of two
+// from 64 that gives at most unitTarget units and fits maxUnits) and each
+// bin's first unit. Contains barriers; the whole CTA calls it.
+__device__ void planUnits(const DrawDev& d, S32* s_scratch) {
+    const S64 total = __ldcg(&d.counters->binEntries);
+    S64 U = d.unitEntries;
+    if (U <= 0) {
+        const S64 room = max((S64)1, d.maxUnits - d.totalBins - 1);
+        U = 64;
+        while (U < 4096 && total > (S64)max(d.unitTarget, 1) * U) U *= 2;
+        while (total > room * U && U < ((S64)1 << 30)) U *= 2;
+    }
+    S32 carry = 0;
+    for (int b0 = 0; b0 < d.totalBins; b0 += kBinThreads) {
+        const int b = b0 + threadIdx.x;
+        const S32 n = b < d.totalBins ? (S32)(((S64)__ldcg(&d.binCount[b]) + U - 1) / U) : 0;
+        S32 tot;
+        const S32 ex = blockExclusiveScan(n, s_scratch, &tot);
+        if (b < d.totalBins) d.binUnitFirst[b] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) {
+        d.counters->unitEntries = (S32)U;
+        d.counters->numUnits = carry;
+    }
+}
+
+// One CTA per global bin: chunk-order exclusive offsets and list allocation;
+// the last CTA to finish plans the coarse units.
 __global__ void __launch_bounds__(kBinThreads) binScanKernel(DrawDev d) {
     __shared__ S32 s_scratch[kBinWarps + 1];
     __shared__ int s_inst;
-    __shared__ S32 s_units, s_unitFirst;
+    __shared__ bool s_last;
     if (__ldg(&d.counters->overflow) & kOverflowSubtris) return;
     const int gb = blockIdx.x;
     if (threadIdx.x == 0) s_inst = findInstance(d.binPrefix, d.numInstances, gb);
@@ -278,19 +307,13 @@ __global__ void __launch_bounds__(kBinThreads) binScanKernel(DrawDev d) {
         if ((S64)start + carry > d.maxBinEntries) atomicOr(&d.counters->overflow, kOverflowBin);
         d.binStart[gb] = start;
         d.binCount[gb] = carry;
-        S32 units = (carry + d.unitEntries - 1) / d.unitEntries;
-        S32 first = atomicAdd(&d.counters->numUnits, units);
-        d.binUnitFirst[gb] = first;
-        s_units = units;
-        s_unitFirst = first;
+        __threadfence();
+        s_last = atomicAdd(&d.counters->binsDone, 1) == d.totalBins - 1;
     }
     __syncthreads();
-    const S32 units = s_units, first = s_unitFirst;
-    for (int k = threadIdx.x; k < units; k += kBinThreads) {
-        if ((S64)first + k < d.maxUnits) {
-            d.unitBin[first + k] = gb;
-            d.unitSeg[first + k] = k;
-        }
+    if (s_last) {
+        __threadfence();
+        planUnits(d, s_scratch);
     }
 }
 
@@ -428,34 +451,110 @@ __global__ void __launch_bounds__(kBinThreads, 2) binScatterKernel(DrawDev d) {
 }
 
 // --------------------------------------------------------------- coarse
+//
+// A coarse unit (up to unitEntries consecutive entries of one bin list) is
+// taken by one warp, which walks it 32 entries (a group) at a time. A group is
+// expanded into (entry, tile) pairs -- every tile of each entry's bounding
+// box inside the bin -- and the pairs are dealt evenly over the lanes, so an
+// entry covering many tiles costs its tile count / 32 iterations instead of
+// holding up the whole warp. No CTA-wide barrier is involved: units, groups
+// and ranks are all warp-local.
+
+constexpr int kCoarseThreads = 256;
+constexpr int kCoarseWarps = kCoarseThreads / 32;
+
+// The current group of a warp, one word per entry (lane).
+struct GroupSmem {
+    S32 incl[32];   // inclusive prefix of the entries' box tile counts
+    U32 v[3][32];   // vertices, packed as in the triangle header
+    U32 box[32];    // lx | ly << 8 | w << 16 (bin-local tiles), bit 31: box of at most 2x2 tiles
+    U32 mul[32];    // ceil(2^20 / w): tile k of the box is in row (k * mul) >> 20
+    U32 entry[32];
+};
+
+// Loads the group's entries (lane i: list position e0 + i, valid below e1)
+// and publishes them; returns the group's number of pairs.
+__device__ __forceinline__ S32 stageGroup(const DrawDev& d, const Grid& gr, S32 e, S32 e1, GroupSmem& gs, S32& incl) {
+    const int lane = threadIdx.x & 31;
+    S32 n = 0;
+    U32 entry = 0, box = 0, mul = 0;
+    uint4 h = make_uint4(0u, 0u, 0u, 0u);
+    if (e < e1) {
+        entry = __ldg(&d.binList[e]);
+        h = __ldg(&d.triHeader[entrySlot(entry, d.triHeader)]);
+        const CellBox b = cellBox(geomFromHeader(h), gr.halfW, gr.halfH, gr.cellLog2, gr.cx0, gr.cy0, gr.cx1, gr.cy1);
+        n = b.count();
+        if (n > 0) {
+            const U32 w = (U32)(b.hx - b.lx + 1);
+            box = (U32)(b.lx - gr.cx0) | (U32)(b.ly - gr.cy0) << 8 | w << 16 | (b.small() ? 1u << 31 : 0u);
+            mul = ((1u << 20) + w - 1u) / w;
+        }
+    }
+    incl = warpInclusiveScan(n);
+    gs.incl[lane] = incl;
+    gs.v[0][lane] = h.x;
+    gs.v[1][lane] = h.y;
+    gs.v[2][lane] = h.z;
+    gs.box[lane] = box;
+    gs.mul[lane] = mul;
+    gs.entry[lane] = entry;
+    __syncwarp();
+    return __shfl_sync(0xFFFFFFFFu, incl, 31);
+}
+
+// Pair p of the group (p below the group's pair count): its entry j and its
+// bin-local cell; returns whether the entry's triangle may touch the tile.
+// The quotient k / w is exact for k < 2^10 and w <= 32 (error below 2^-10).
+__device__ __forceinline__ bool pairCell(const GroupSmem& gs, const Grid& gr, S32 p, int& j, int& cell) {
+    int jj = 0;
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1)
+        if (gs.incl[jj + s - 1] <= p) jj += s;
+    const S32 k = p - (jj ? gs.incl[jj - 1] : 0);
+    const U32 box = gs.box[jj];
+    const S32 w = (S32)((box >> 16) & 0xFFu);
+    const S32 q = (S32)(((U32)k * gs.mul[jj]) >> 20);
+    const S32 lx = (S32)(box & 0xFFu) + k - q * w;
+    const S32 ly = (S32)((box >> 8) & 0xFFu) + q;
+    j = jj;
+    cell = ly * gr.stride + lx;
+    if (box >> 31) return true;
+    const TriGeom g = geomFromHeader(make_uint4(gs.v[0][jj], gs.v[1][jj], gs.v[2][jj], 0u));
+    const S32 side = 1 << gr.cellLog2;
+    const S32 rx0 = ((gr.cx0 + lx) << gr.cellLog2) - gr.halfW, ry0 = ((gr.cy0 + ly) << gr.cellLog2) - gr.halfH;
+    return triTouchesRect(g, rx0, ry0, rx0 + side - 1, ry0 + side - 1);
+}
 
 struct UnitInfo {
     const InstanceDev* in;
     S32 gb, seg, bx, by, e0, e1;
 };
 
-// Next coarse unit for this CTA (dynamic assignment, so CTAs that drew heavy
-// units take fewer). Contains a barrier; the result is uniform.
-__device__ __forceinline__ int nextUnit(S32* counter, int* s_unit) {
-    __syncthreads();
-    if (threadIdx.x == 0) *s_unit = atomicAdd(counter, 1);
-    __syncthreads();
-    return *s_unit;
+// Next coarse unit for this warp (dynamic assignment); uniform across the warp.
+__device__ __forceinline__ int warpNextUnit(S32* counter) {
+    int u = 0;
+    if ((threadIdx.x & 31) == 0) u = atomicAdd(counter, 1);
+    return __shfl_sync(0xFFFFFFFFu, u, 0);
 }
 
-__device__ __forceinline__ void loadUnit(const DrawDev& d, int u, UnitInfo& ui, int* s_inst) {
-    if (threadIdx.x == 0) *s_inst = findInstance(d.binPrefix, d.numInstances, __ldg(&d.unitBin[u]));
-    __syncthreads();
-    ui.in = &d.inst[*s_inst];
-    ui.gb = __ldg(&d.unitBin[u]);
-    ui.seg = __ldg(&d.unitSeg[u]);
-    S32 b = ui.gb - __ldg(&ui.in->binBase);
-    S32 wb = __ldg(&ui.in->widthBins);
+// Unit u: the last bin whose first unit is at most u (bins without units
+// share their first unit with the next bin), and its entry range.
+__device__ __forceinline__ void loadUnit(const DrawDev& d, int u, S32 unitEntries, UnitInfo& ui) {
+    int lo = 0, hi = d.totalBins - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&d.binUnitFirst[mid]) <= u) lo = mid; else hi = mid - 1;
+    }
+    ui.gb = lo;
+    ui.in = &d.inst[findInstance(d.binPrefix, d.numInstances, ui.gb)];
+    ui.seg = u - __ldg(&d.binUnitFirst[lo]);
+    const S32 b = ui.gb - __ldg(&ui.in->binBase);
+    const S32 wb = __ldg(&ui.in->widthBins);
     ui.bx = b % wb;
     ui.by = b / wb;
-    S32 start = __ldg(&d.binStart[ui.gb]), cnt = __ldg(&d.binCount[ui.gb]);
-    ui.e0 = start + ui.seg * d.unitEntries;
-    ui.e1 = min(ui.e0 + d.unitEntries, start + cnt);
+    const S32 start = __ldg(&d.binStart[ui.gb]), cnt = __ldg(&d.binCount[ui.gb]);
+    ui.e0 = start + ui.seg * unitEntries;
+    ui.e1 = min(ui.e0 + unitEntries, start + cnt);
 }
 
 __device__ __forceinline__ Grid tileGrid(const UnitInfo& ui, int binLog2) {
@@ -472,37 +571,37 @@ __device__ __forceinline__ Grid tileGrid(const UnitInfo& ui, int binLog2) {
     return gr;
 }
 
-// Persistent CTAs over coarse units (taken dynamically): per-unit tile counts.
-__global__ void __launch_bounds__(kBinThreads, 2) coarseCountKernel(DrawDev d) {
-    extern __shared__ S32 s_count[];
-    __shared__ RoundShared rs;
-    __shared__ int s_inst;
+// Persistent warps over coarse units (taken dynamically): per-unit tile counts.
+__global__ void __launch_bounds__(kCoarseThreads) coarseCountKernel(DrawDev d) {
+    extern __shared__ S32 smem[];
+    __shared__ GroupSmem s_group[kCoarseWarps];
     if (__ldg(&d.counters->overflow) & (kOverflowSubtris | kOverflowBin)) return;
-    __shared__ int s_unit;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int tpb = 1 << (2 * d.binLog2);
-    const S32 numUnits = (S32)min((S64)*(volatile S32*)&d.counters->numUnits, d.maxUnits);
+    S32* cnt = smem + warp * tpb;
+    GroupSmem& gs = s_group[warp];
+    const S32 numUnits = (S32)min((S64)__ldg(&d.counters->numUnits), d.maxUnits);
+    const S32 unitEntries = __ldg(&d.counters->unitEntries);
     for (;;) {
-        const int u = nextUnit(&d.counters->coarseWork[0], &s_unit);
+        const int u = warpNextUnit(&d.counters->coarseWork[0]);
         if (u >= numUnits) break;
         UnitInfo ui;
-        loadUnit(d, u, ui, &s_inst);
-        for (int t = threadIdx.x; t < tpb; t += kBinThreads) s_count[t] = 0;
+        loadUnit(d, u, unitEntries, ui);
         const Grid gr = tileGrid(ui, d.binLog2);
-        __syncthreads();
-        for (S32 e0 = ui.e0; e0 < ui.e1; e0 += kBinThreads) {
-            const S32 e = e0 + threadIdx.x;
-            const bool valid = e < ui.e1;
-            U32 entry = 0;
-            TriGeom g{};
-            if (valid) {
-                entry = __ldg(&d.binList[e]);
-                g = geomFromHeader(d.triHeader[entrySlot(entry, d.triHeader)]);
+        for (int t = lane; t < tpb; t += 32) cnt[t] = 0;
+        __syncwarp();
+        for (S32 e0 = ui.e0; e0 < ui.e1; e0 += 32) {
+            S32 incl;
+            const S32 P = stageGroup(d, gr, e0 + lane, ui.e1, gs, incl);
+            for (S32 p = lane; p < P; p += 32) {
+                int j, cell;
+                if (pairCell(gs, gr, p, j, cell)) atomicAdd(&cnt[cell], 1);
             }
-            visitRound(rs, valid, g, entry, gr, true, [&](int cell, S32, U32) { atomicAdd(&s_count[cell], 1); });
-            __syncthreads();
+            __syncwarp();
         }
-        for (int t = threadIdx.x; t < tpb; t += kBinThreads) d.unitTileCount[(S64)u * tpb + t] = s_count[t];
-        __syncthreads();
+        S32* out = d.unitTileCount + (S64)u * tpb;
+        for (int t = lane; t < tpb; t += 32) out[t] = cnt[t];
+        __syncwarp();
     }
 }
 
@@ -524,17 +623,30 @@ __global__ void __launch_bounds__(kBinThreads) coarseScanKernel(DrawDev d) {
     const S32 wt = __ldg(&in->widthTiles), ht = __ldg(&in->heightTiles);
     const S32 tileBase = __ldg(&in->tileBase);
     const S32 cnt = __ldg(&d.binCount[gb]);
-    const S32 units = (cnt + d.unitEntries - 1) / d.unitEntries;
+    const S32 unitEntries = __ldg(&d.counters->unitEntries);
+    const S32 units = (cnt + unitEntries - 1) / unitEntries;
     const S32 first = __ldg(&d.binUnitFirst[gb]);
     S32 carry = 0;
     for (int t0 = 0; t0 < tpb; t0 += kBinThreads) {
         int t = t0 + threadIdx.x;
         S32 acc = 0;
         if (t < tpb) {
-            for (S32 k = 0; k < units; k++) {
-                S32* p = &d.unitTileCount[(S64)(first + k) * tpb + t];
-                S32 c = *p;
-                *p = acc;
+            S32* col = d.unitTileCount + (S64)first * tpb + t;
+            // Eight units per step: the loads are issued before the stores.
+            S32 k = 0;
+            for (; k + 8 <= units; k += 8) {
+                S32 c[8];
+#pragma unroll
+                for (int i = 0; i < 8; i++) c[i] = col[(S64)(k + i) * tpb];
+#pragma unroll
+                for (int i = 0; i < 8; i++) {
+                    col[(S64)(k + i) * tpb] = acc;
+                    acc += c[i];
+                }
+            }
+            for (; k < units; k++) {
+                const S32 c = col[(S64)k * tpb];
+                col[(S64)k * tpb] = acc;
                 acc += c;
             }
         }
@@ -564,46 +676,83 @@ __global__ void __launch_bounds__(kBinThreads) coarseScanKernel(DrawDev d) {
     }
 }
 
-// Persistent CTAs over coarse units (taken dynamically): writes tile list
-// entries, ranked per 512-entry round by per-warp ballot masks over the tiles
-// of the bin.
-__global__ void __launch_bounds__(kBinThreads, 2) coarseScatterKernel(DrawDev d) {
+// Persistent warps over coarse units (taken dynamically): writes tile list
+// entries. Within a group the rank of an entry in a tile list is the number of
+// earlier entries of the group touching the tile (a per-tile mask, one bit per
+// entry) plus the tile's running index. A group whose pairs exceed the per-
+// warp hit buffer (one slot per tile of the bin) is taken in sub-groups that
+// end at entry boundaries; one entry never has more pairs than the bin has
+// tiles.
+__global__ void __launch_bounds__(kCoarseThreads) coarseScatterKernel(DrawDev d) {
     extern __shared__ S32 smem[];
-    __shared__ RoundShared rs;
-    __shared__ int s_inst;
+    __shared__ GroupSmem s_group[kCoarseWarps];
     if (__ldg(&d.counters->overflow) & (kOverflowSubtris | kOverflowBin | kOverflowTile)) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const U32 ltMask = (1u << lane) - 1u;
     const int tpb = 1 << (2 * d.binLog2);
     const S32 side = 1 << d.binLog2;
-    __shared__ int s_unit;
-    const ScatterSmem sm = carveScatter(smem, tpb);
-    const S32 numUnits = (S32)min((S64)*(volatile S32*)&d.counters->numUnits, d.maxUnits);
-    clearScatter(sm);
+    U32* mask = (U32*)smem + (size_t)warp * 3 * tpb;   // [tpb] entries of the sub-group per tile
+    S32* run = (S32*)(mask + tpb);                      // [tpb] next free list index per tile
+    U32* hits = (U32*)(run + tpb);                      // [tpb] cell | entry << 16 of touching pairs
+    GroupSmem& gs = s_group[warp];
+    for (int t = lane; t < tpb; t += 32) mask[t] = 0u;
+    const S32 numUnits = (S32)min((S64)__ldg(&d.counters->numUnits), d.maxUnits);
+    const S32 unitEntries = __ldg(&d.counters->unitEntries);
     for (;;) {
-        const int u = nextUnit(&d.counters->coarseWork[1], &s_unit);
+        const int u = warpNextUnit(&d.counters->coarseWork[1]);
         if (u >= numUnits) break;
         UnitInfo ui;
-        loadUnit(d, u, ui, &s_inst);
+        loadUnit(d, u, unitEntries, ui);
         const Grid gr = tileGrid(ui, d.binLog2);
         const S32 wt = __ldg(&ui.in->widthTiles);
         const S32 tileBase = __ldg(&ui.in->tileBase);
-        for (int t = threadIdx.x; t < tpb; t += kBinThreads) {
-            S32 tx = gr.cx0 + (t & (side - 1)), ty = gr.cy0 + (t >> d.binLog2);
+        const S32* unitCount = d.unitTileCount + (S64)u * tpb;
+        for (int t = lane; t < tpb; t += 32) {
+            const S32 tx = gr.cx0 + (t & (side - 1)), ty = gr.cy0 + (t >> d.binLog2);
             S32 v = 0;
-            if (tx <= gr.cx1 && ty <= gr.cy1)
-                v = __ldg(&d.tileStart[tileBase + ty * wt + tx]) + __ldg(&d.unitTileCount[(S64)u * tpb + t]);
-            sm.run[t] = v;
+            if (tx <= gr.cx1 && ty <= gr.cy1) v = __ldg(&d.tileStart[tileBase + ty * wt + tx]) + __ldg(&unitCount[t]);
+            run[t] = v;
         }
-        __syncthreads();
-        for (S32 e0 = ui.e0; e0 < ui.e1; e0 += kBinThreads) {
-            const S32 e = e0 + threadIdx.x;
-            const bool valid = e < ui.e1;
-            U32 entry = 0;
-            TriGeom g{};
-            if (valid) {
-                entry = __ldg(&d.binList[e]);
-                g = geomFromHeader(d.triHeader[entrySlot(entry, d.triHeader)]);
+        __syncwarp();
+        for (S32 e0 = ui.e0; e0 < ui.e1; e0 += 32) {
+            S32 incl;
+            const S32 P = stageGroup(d, gr, e0 + lane, ui.e1, gs, incl);
+            for (S32 p0 = 0; p0 < P;) {
+                // Entries whose pairs all lie below p0 + tpb form the sub-group.
+                const int jEnd = __popc(__ballot_sync(0xFFFFFFFFu, incl <= p0 + tpb));
+                const S32 p1 = __shfl_sync(0xFFFFFFFFu, incl, jEnd - 1);
+                S32 nh = 0;
+                for (S32 base = p0; base < p1; base += 32) {
+                    const S32 p = base + lane;
+                    int j = 0, cell = 0;
+                    const bool hit = p < p1 && pairCell(gs, gr, p, j, cell);
+                    if (hit) atomicOr(&mask[cell], 1u << j);
+                    const U32 b = __ballot_sync(0xFFFFFFFFu, hit);
+                    if (hit) hits[nh + __popc(b & ltMask)] = (U32)cell | (U32)j << 16;
+                    nh += __popc(b);
+                }
+                __syncwarp();
+                for (S32 h = lane; h < nh; h += 32) {
+                    const U32 hc = hits[h];
+                    const int cell = (int)(hc & 0xFFFFu), j = (int)(hc >> 16);
+                    const S64 idx = (S64)run[cell] + __popc(mask[cell] & ((1u << j) - 1u));
+                    if (idx < d.maxTileEntries) d.tileList[idx] = gs.entry[j];
+                }
+                __syncwarp();
+                // The last entry of the sub-group touching a tile advances the
+                // tile's index and clears its mask.
+                for (S32 h = lane; h < nh; h += 32) {
+                    const U32 hc = hits[h];
+                    const int cell = (int)(hc & 0xFFFFu), j = (int)(hc >> 16);
+                    const U32 m = mask[cell];
+                    if ((m >> j) == 1u) {
+                        run[cell] += __popc(m);
+                        mask[cell] = 0u;
+                    }
+                }
+                __syncwarp();
+                p0 = p1;
             }
-            scatterRound<false>(rs, valid, g, entry, gr, sm, d.tileList, d.maxTileEntries);
         }
     }
 }
@@ -611,28 +760,45 @@ __global__ void __launch_bounds__(kBinThreads, 2) coarseScatterKernel(DrawDev d)
 // ------------------------------------------------------------ launchers
 
 size_t binScatterSmem(int maxBins) { return scatterSmemBytes(maxBins); }
-size_t coarseScatterSmem(int binLog2) { return scatterSmemBytes(1 << (2 * binLog2)); }
+size_t coarseCountSmem(int binLog2) { return sizeof(S32) * kCoarseWarps * ((size_t)1 << (2 * binLog2)); }
+size_t coarseScatterSmem(int binLog2) { return sizeof(S32) * 3 * kCoarseWarps * ((size_t)1 << (2 * binLog2)); }
 
 cudaError_t launchBinning(const DrawDev& d, int maxBins, int numSMs, cudaStream_t stream, cudaEvent_t evCoarse) {
+    // Resident coarse CTAs per SM for bins of 8, 16 and 32 tiles a side.
+    static int coarseCountCtas[6] = {}, coarseScatterCtas[6] = {};
     static bool configured = false;
     if (!configured) {
         cudaFuncSetAttribute(binScatterKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
         cudaFuncSetAttribute(coarseScatterKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
         cudaFuncSetAttribute(binCountKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
         cudaFuncSetAttribute(coarseCountKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
+        for (int b = 3; b <= 5; b++) {
+            int n = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, coarseCountKernel, kCoarseThreads, coarseCountSmem(b));
+            coarseCountCtas[b] = n > 0 ? n : 1;
+            n = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, coarseScatterKernel, kCoarseThreads, coarseScatterSmem(b));
+            coarseScatterCtas[b] = n > 0 ? n : 1;
+        }
         configured = true;
     }
-    const int tpb = 1 << (2 * d.binLog2);
+    const int bl = d.binLog2 >= 3 && d.binLog2 <= 5 ? d.binLog2 : 4;
+    // Units sized on the device: about two per resident coarse-scatter warp.
+    DrawDev dl = d;
+    dl.unitTarget = 2 * numSMs * coarseScatterCtas[bl] * kCoarseWarps;
     // binScan also runs for a draw without triangles: it zeroes the bin counts.
-    if (d.totalChunks > 0) binCountKernel<<<d.totalChunks, kBinThreads, sizeof(S32) * maxBins, stream>>>(d);
-    binScanKernel<<<d.totalBins, kBinThreads, 0, stream>>>(d);
-    if (d.totalChunks > 0) binScatterKernel<<<d.totalChunks, kBinThreads, binScatterSmem(maxBins), stream>>>(d);
+    if (dl.totalChunks > 0) binCountKernel<<<dl.totalChunks, kBinThreads, sizeof(S32) * maxBins, stream>>>(dl);
+    binScanKernel<<<dl.totalBins, kBinThreads, 0, stream>>>(dl);
+    if (dl.totalChunks > 0) binScatterKernel<<<dl.totalChunks, kBinThreads, binScatterSmem(maxBins), stream>>>(dl);
     if (evCoarse) cudaEventRecord(evCoarse, stream);
-    // Persistent coarse CTAs: as many as are resident at once (2 per SM).
-    const int coarseGrid = numSMs * 2;
-    coarseCountKernel<<<coarseGrid, kBinThreads, sizeof(S32) * tpb, stream>>>(d);
-    coarseScanKernel<<<d.totalBins, kBinThreads, 0, stream>>>(d);
-    coarseScatterKernel<<<coarseGrid, kBinThreads, coarseScatterSmem(d.binLog2), stream>>>(d);
+    // Persistent coarse warps: as many CTAs as are resident at once, and no
+    // more than the draw's units can keep busy.
+    const S64 unitCtas = (dl.maxUnits + kCoarseWarps - 1) / kCoarseWarps;
+    const int countGrid = (int)min((S64)numSMs * coarseCountCtas[bl], unitCtas);
+    const int scatterGrid = (int)min((S64)numSMs * coarseScatterCtas[bl], unitCtas);
+    coarseCountKernel<<<countGrid, kCoarseThreads, coarseCountSmem(dl.binLog2), stream>>>(dl);
+    coarseScanKernel<<<dl.totalBins, kBinThreads, 0, stream>>>(dl);
+    coarseScatterKernel<<<scatterGrid, kCoarseThreads, coarseScatterSmem(dl.binLog2), stream>>>(dl);
     return cudaGetLastError();
 }
 

@@ -111,7 +111,7 @@ struct cr_context {
     bool userCapacity = false;  // capacities set by cr_set_capacity replace the estimates
     // Device memory.
     DevBuf triSubtris, triHeader, triData, chunkBinCount, binCount, binStart, binUnitFirst, binList;
-    DevBuf unitBin, unitSeg, unitTileCount, tileCount, tileStart, tileList;
+    DevBuf unitTileCount, tileCount, tileStart, tileList;
     DevBuf instBuf;   // instance descriptors, then the prefix arrays (one copy per draw)
     DevBuf counters;  // Counters, then one fine-stage tile counter per pipe group (one memset per draw)
     // Pinned staging.
@@ -248,8 +248,8 @@ cr_status cr_destroy(cr_context* ctx) {
     if (!ctx) return CR_ERR_INVALID_ARGUMENT;
     cudaDeviceSynchronize();
     DevBuf* bufs[] = {&ctx->triSubtris, &ctx->triHeader, &ctx->triData, &ctx->chunkBinCount, &ctx->binCount,
-                      &ctx->binStart, &ctx->binUnitFirst, &ctx->binList, &ctx->unitBin, &ctx->unitSeg,
-                      &ctx->unitTileCount, &ctx->tileCount, &ctx->tileStart, &ctx->tileList, &ctx->instBuf,
+                      &ctx->binStart, &ctx->binUnitFirst, &ctx->binList, &ctx->unitTileCount,
+                      &ctx->tileCount, &ctx->tileStart, &ctx->tileList, &ctx->instBuf,
                       &ctx->counters};
     for (DevBuf* b : bufs) b->release();
     for (int i = 0; i < cr_context::kStageSlots; i++) {
@@ -395,12 +395,21 @@ struct Plan {
     std::vector<Group> groups;
     int64_t totalTris = 0, chunkCountEntries = 0;
     int32_t totalBins = 0, totalTiles = 0, totalChunks = 0, maxBins = 0;
-    int binLog2 = 4, unitEntries = 2048;
+    int binLog2 = 4, unitEntries = 0;
 };
+
+// Coarse units a draw may use. A unit size set by the caller bounds them by
+// the bin capacity; units sized on the device (unitEntries 0, at least 64
+// entries each) are also capped at 8M per-unit tile counters, and the device
+// grows the unit size until the draw's bin entries fit.
+int64_t unitCapacity(int64_t maxBinEntries, int unitEntries, int32_t totalBins, int tpb) {
+    if (unitEntries > 0) return maxBinEntries / unitEntries + totalBins + 1;
+    return std::min<int64_t>(maxBinEntries / 64, std::max<int64_t>(4096, (8 << 20) / tpb)) + totalBins + 1;
+}
 
 cr_status buildPlan(cr_context* ctx, const std::vector<HostInstance>& in, Plan& plan) {
     plan.binLog2 = ctx->tuning.bin_log2 > 0 ? ctx->tuning.bin_log2 : 4;
-    plan.unitEntries = ctx->tuning.coarse_unit_entries > 0 ? ctx->tuning.coarse_unit_entries : 512;
+    plan.unitEntries = std::max(0, ctx->tuning.coarse_unit_entries);   // 0: sized on the device
     // Group instances by pipe, keeping first-seen pipe order (outputs do not depend on it).
     std::vector<const PipeDesc*> order;
     for (const HostInstance& h : in)
@@ -495,7 +504,7 @@ cr_status ensureCapacity(cr_context* ctx, const Plan& plan) {
         ctx->maxTileEntries = std::max<int64_t>(ctx->maxTileEntries, 4 * T + 65536);
     }
     const int tpb = 1 << (2 * plan.binLog2);
-    int64_t maxUnits = ctx->maxBinEntries / plan.unitEntries + plan.totalBins + 1;
+    const int64_t maxUnits = unitCapacity(ctx->maxBinEntries, plan.unitEntries, plan.totalBins, tpb);
     CR_CUDA(ctx->triSubtris.ensure((size_t)std::max<int64_t>(T, 1)), "cudaMalloc");
     CR_CUDA(ctx->triHeader.ensure((size_t)ctx->maxSubtris * 16), "cudaMalloc");
     CR_CUDA(ctx->triData.ensure((size_t)ctx->maxSubtris * 64), "cudaMalloc");
@@ -504,8 +513,6 @@ cr_status ensureCapacity(cr_context* ctx, const Plan& plan) {
     CR_CUDA(ctx->binStart.ensure((size_t)plan.totalBins * 4), "cudaMalloc");
     CR_CUDA(ctx->binUnitFirst.ensure((size_t)plan.totalBins * 4), "cudaMalloc");
     CR_CUDA(ctx->binList.ensure((size_t)ctx->maxBinEntries * 4), "cudaMalloc");
-    CR_CUDA(ctx->unitBin.ensure((size_t)maxUnits * 4), "cudaMalloc");
-    CR_CUDA(ctx->unitSeg.ensure((size_t)maxUnits * 4), "cudaMalloc");
     CR_CUDA(ctx->unitTileCount.ensure((size_t)maxUnits * tpb * 4), "cudaMalloc");
     CR_CUDA(ctx->tileCount.ensure((size_t)plan.totalTiles * 4), "cudaMalloc");
     CR_CUDA(ctx->tileStart.ensure((size_t)plan.totalTiles * 4), "cudaMalloc");
@@ -554,10 +561,8 @@ DrawDev makeDrawDev(cr_context* ctx, const Plan& plan) {
     d.binUnitFirst = ctx->binUnitFirst.as<int32_t>();
     d.binList = ctx->binList.as<uint32_t>();
     d.maxBinEntries = ctx->maxBinEntries;
-    d.unitBin = ctx->unitBin.as<int32_t>();
-    d.unitSeg = ctx->unitSeg.as<int32_t>();
     d.unitTileCount = ctx->unitTileCount.as<int32_t>();
-    d.maxUnits = ctx->maxBinEntries / plan.unitEntries + plan.totalBins + 1;
+    d.maxUnits = unitCapacity(ctx->maxBinEntries, plan.unitEntries, plan.totalBins, 1 << (2 * plan.binLog2));
     d.tileCount = ctx->tileCount.as<int32_t>();
     d.tileStart = ctx->tileStart.as<int32_t>();
     d.tileList = ctx->tileList.as<uint32_t>();

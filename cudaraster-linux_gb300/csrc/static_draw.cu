@@ -76,9 +76,7 @@ constexpr size_t kOffBinCount = alignUp(kOffChunkCount + 4 * (size_t)kStaticMaxC
 constexpr size_t kOffBinStart = alignUp(kOffBinCount + 4 * kStaticMaxBins);
 constexpr size_t kOffBinUnitFirst = alignUp(kOffBinStart + 4 * kStaticMaxBins);
 constexpr size_t kOffBinList = alignUp(kOffBinUnitFirst + 4 * kStaticMaxBins);
-constexpr size_t kOffUnitBin = alignUp(kOffBinList + 4 * kStaticMaxBinEntries);
-constexpr size_t kOffUnitSeg = alignUp(kOffUnitBin + 4 * kStaticMaxUnits);
-constexpr size_t kOffUnitTileCount = alignUp(kOffUnitSeg + 4 * kStaticMaxUnits);
+constexpr size_t kOffUnitTileCount = alignUp(kOffBinList + 4 * kStaticMaxBinEntries);
 constexpr size_t kOffTileCount = alignUp(kOffUnitTileCount + 4 * (size_t)kStaticMaxUnits * kStaticTilesPerBin);
 constexpr size_t kOffTileStart = alignUp(kOffTileCount + 4 * kStaticMaxTiles);
 constexpr size_t kOffTileList = alignUp(kOffTileStart + 4 * kStaticMaxTiles);
@@ -218,8 +216,6 @@ extern "C" cr_status cr_draw_triangles_static(const char* pipe_name, void* color
     d.binUnitFirst = (int32_t*)(scratch + kOffBinUnitFirst);
     d.binList = (uint32_t*)(scratch + kOffBinList);
     d.maxBinEntries = kStaticMaxBinEntries;
-    d.unitBin = (int32_t*)(scratch + kOffUnitBin);
-    d.unitSeg = (int32_t*)(scratch + kOffUnitSeg);
     d.unitTileCount = (int32_t*)(scratch + kOffUnitTileCount);
     d.maxUnits = kStaticMaxUnits;
     d.tileCount = (int32_t*)(scratch + kOffTileCount);

@@ -84,6 +84,8 @@ struct Counters {
     S32 fineTile;             // fine-stage work counter
     S32 overflow;             // kOverflow* bits
     S32 coarseWork[2];        // coarse count / scatter unit counters (dynamic unit assignment)
+    S32 binsDone;             // bin-scan CTAs finished (the last one plans the coarse units)
+    S32 unitEntries;          // bin entries per coarse unit, as planned for this draw
 };
 
 // Buffers shared by every instance of a draw.
@@ -94,7 +96,8 @@ struct DrawDev {
     S32 totalBins;
     S32 totalTiles;
     S32 totalChunks;
-    S32 unitEntries;          // bin entries per coarse unit
+    S32 unitEntries;          // bin entries per coarse unit; <= 0: sized on the device from the bin entries
+    S32 unitTarget;           // coarse units wanted when sized on the device (set by the launcher)
     S64 totalTris;
     // setup
     uint8_t* triSubtris;      // [totalTris]
@@ -110,8 +113,6 @@ struct DrawDev {
     U32* binList;             // [maxBinEntries]
     S64 maxBinEntries;
     // coarse
-    S32* unitBin;             // [maxUnits] global bin of the unit
-    S32* unitSeg;             // [maxUnits] segment index inside the bin
     S32* unitTileCount;       // [maxUnits << 2*binLog2]: count, then offset
     S64 maxUnits;
     S32* tileCount;           // [totalTiles]
