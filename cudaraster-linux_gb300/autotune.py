@@ -27,7 +27,7 @@ def candidates(quick: bool = False):
     bins = (3, 4, 5)
     warps = (4, 8)
     units = (0, 64, 128, 256, 512, 1024) if not quick else (0,)
-    chunks = (0, 1024, 4096) if not quick else (0,)
+    chunks = (0, 256, 1024, 4096) if not quick else (0,)
     for b, w, u, c in itertools.product(bins, warps, units, chunks):
         yield {"bin_log2": b, "fine_warps": w, "coarse_unit_entries": u, "bin_chunk_tris": c}
 

@@ -75,6 +75,12 @@ struct DevBuf {
         if (e == cudaSuccess) bytes = alloc;
         return e;
     }
+    // As ensure, and a new allocation starts zeroed.
+    cudaError_t ensureZeroed(size_t need) {
+        if (need <= bytes) return cudaSuccess;
+        cudaError_t e = ensure(need);
+        return e == cudaSuccess ? cudaMemset(ptr, 0, bytes) : e;
+    }
     void release() {
         if (ptr) cudaFree(ptr);
         ptr = nullptr;
@@ -110,7 +116,7 @@ struct cr_context {
     int64_t maxSubtris = 0, maxBinEntries = 0, maxTileEntries = 0;
     bool userCapacity = false;  // capacities set by cr_set_capacity replace the estimates
     // Device memory.
-    DevBuf triSubtris, triHeader, triData, chunkBinCount, binCount, binStart, binUnitFirst, binList;
+    DevBuf triSubtris, triHeader, triData, chunkBinCount, chunkBinOffset, binCount, binStart, binUnitFirst, binList;
     DevBuf unitTileCount, tileCount, tileStart, tileList;
     DevBuf instBuf;   // instance descriptors, then the prefix arrays (one copy per draw)
     DevBuf counters;  // Counters, then one fine-stage tile counter per pipe group (one memset per draw)
@@ -247,7 +253,8 @@ cr_status cr_create(cr_context** out) {
 cr_status cr_destroy(cr_context* ctx) {
     if (!ctx) return CR_ERR_INVALID_ARGUMENT;
     cudaDeviceSynchronize();
-    DevBuf* bufs[] = {&ctx->triSubtris, &ctx->triHeader, &ctx->triData, &ctx->chunkBinCount, &ctx->binCount,
+    DevBuf* bufs[] = {&ctx->triSubtris, &ctx->triHeader, &ctx->triData, &ctx->chunkBinCount, &ctx->chunkBinOffset,
+                      &ctx->binCount,
                       &ctx->binStart, &ctx->binUnitFirst, &ctx->binList, &ctx->unitTileCount,
                       &ctx->tileCount, &ctx->tileStart, &ctx->tileList, &ctx->instBuf,
                       &ctx->counters};
@@ -359,8 +366,8 @@ cr_status cr_set_tuning(cr_context* ctx, const cr_tuning* t) {
         return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaRaster: bin_log2 must be 3, 4 or 5");
     if (t->fine_warps > 0 && (t->fine_warps > 8 || (t->fine_warps & (t->fine_warps - 1))))
         return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaRaster: fine_warps must be 1, 2, 4 or 8");
-    if (t->bin_chunk_tris > 0 && (t->bin_chunk_tris % 512))
-        return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaRaster: bin_chunk_tris must be a multiple of 512");
+    if (t->bin_chunk_tris > 0 && (t->bin_chunk_tris % 32))
+        return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaRaster: bin_chunk_tris must be a multiple of 32");
     ctx->tuning = *t;
     return CR_OK;
 }
@@ -418,6 +425,12 @@ cr_status buildPlan(cr_context* ctx, const std::vector<HostInstance>& in, Plan& 
         for (const HostInstance& h : in)
             if (h.pipe == p) plan.inst.push_back(h);
     const int side = 1 << plan.binLog2;
+    // Bin chunks are taken by warps, in order: about 80 per SM (two per
+    // resident bin warp), of 256 to 65536 triangles.
+    int64_t allTris = 0;
+    for (const HostInstance& h : plan.inst) allTris += h.dev.numTris;
+    const int64_t wantChunks = std::max<int64_t>(1, (int64_t)ctx->numSMs * 80);
+    const int autoChunk = (int)std::min<int64_t>(std::max<int64_t>((allTris + wantChunks - 1) / wantChunks, 256), 65536);
     int64_t tri = 0;
     int32_t bins = 0, tiles = 0, chunks = 0;
     int64_t countBase = 0;
@@ -436,14 +449,7 @@ cr_status buildPlan(cr_context* ctx, const std::vector<HostInstance>& in, Plan& 
         d.binBase = bins;
         d.tileBase = tiles;
         int chunkTris = ctx->tuning.bin_chunk_tris;
-        if (chunkTris <= 0) {
-            // Whole waves of the bin CTAs (2 resident per SM), chunks of at most
-            // 65536 and (for small draws) at least 1024 triangles.
-            const int64_t slots = std::max(1, ctx->numSMs * 2);
-            const int64_t waves = std::max<int64_t>(1, ((int64_t)d.numTris + slots * 65536 - 1) / (slots * 65536));
-            const int64_t want = ((int64_t)d.numTris + slots * waves - 1) / (slots * waves);
-            chunkTris = (int)std::min<int64_t>(std::max<int64_t>(want, 1024), 65536);
-        }
+        if (chunkTris <= 0) chunkTris = autoChunk;
         d.chunkTris = chunkTris;
         d.numChunks = (d.numTris + chunkTris - 1) / chunkTris;
         d.chunkBase = chunks;
@@ -508,7 +514,8 @@ cr_status ensureCapacity(cr_context* ctx, const Plan& plan) {
     CR_CUDA(ctx->triSubtris.ensure((size_t)std::max<int64_t>(T, 1)), "cudaMalloc");
     CR_CUDA(ctx->triHeader.ensure((size_t)ctx->maxSubtris * 16), "cudaMalloc");
     CR_CUDA(ctx->triData.ensure((size_t)ctx->maxSubtris * 64), "cudaMalloc");
-    CR_CUDA(ctx->chunkBinCount.ensure((size_t)std::max<int64_t>(plan.chunkCountEntries, 1) * 4), "cudaMalloc");
+    CR_CUDA(ctx->chunkBinCount.ensureZeroed((size_t)std::max<int64_t>(plan.chunkCountEntries, 1) * 4), "cudaMalloc");
+    CR_CUDA(ctx->chunkBinOffset.ensure((size_t)std::max<int64_t>(plan.chunkCountEntries, 1) * 4), "cudaMalloc");
     CR_CUDA(ctx->binCount.ensure((size_t)plan.totalBins * 4), "cudaMalloc");
     CR_CUDA(ctx->binStart.ensure((size_t)plan.totalBins * 4), "cudaMalloc");
     CR_CUDA(ctx->binUnitFirst.ensure((size_t)plan.totalBins * 4), "cudaMalloc");
@@ -556,6 +563,8 @@ DrawDev makeDrawDev(cr_context* ctx, const Plan& plan) {
     d.triData = ctx->triData.as<uint4>();
     d.maxSubtris = ctx->maxSubtris;
     d.chunkBinCount = ctx->chunkBinCount.as<int32_t>();
+    d.chunkBinOffset = ctx->chunkBinOffset.as<int32_t>();
+    d.maxBins = plan.maxBins;
     d.binCount = ctx->binCount.as<int32_t>();
     d.binStart = ctx->binStart.as<int32_t>();
     d.binUnitFirst = ctx->binUnitFirst.as<int32_t>();

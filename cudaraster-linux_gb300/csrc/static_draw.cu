@@ -72,7 +72,8 @@ constexpr size_t kOffSubtris = alignUp(kOffPrefix + 64);
 constexpr size_t kOffHeader = alignUp(kOffSubtris + kStaticMaxTris);
 constexpr size_t kOffData = alignUp(kOffHeader + 16 * kStaticMaxSubtris);
 constexpr size_t kOffChunkCount = alignUp(kOffData + 64 * kStaticMaxSubtris);
-constexpr size_t kOffBinCount = alignUp(kOffChunkCount + 4 * (size_t)kStaticMaxChunks * kStaticMaxBins);
+constexpr size_t kOffChunkOffset = alignUp(kOffChunkCount + 4 * (size_t)kStaticMaxChunks * kStaticMaxBins);
+constexpr size_t kOffBinCount = alignUp(kOffChunkOffset + 4 * (size_t)kStaticMaxChunks * kStaticMaxBins);
 constexpr size_t kOffBinStart = alignUp(kOffBinCount + 4 * kStaticMaxBins);
 constexpr size_t kOffBinUnitFirst = alignUp(kOffBinStart + 4 * kStaticMaxBins);
 constexpr size_t kOffBinList = alignUp(kOffBinUnitFirst + 4 * kStaticMaxBins);
@@ -210,7 +211,9 @@ extern "C" cr_status cr_draw_triangles_static(const char* pipe_name, void* color
     d.triHeader = (uint4*)(scratch + kOffHeader);
     d.triData = (uint4*)(scratch + kOffData);
     d.maxSubtris = kStaticMaxSubtris;
-    d.chunkBinCount = (int32_t*)(scratch + kOffChunkCount);
+    d.chunkBinCount = (int32_t*)(scratch + kOffChunkCount);   // zero at load; each bin scan clears it again
+    d.chunkBinOffset = (int32_t*)(scratch + kOffChunkOffset);
+    d.maxBins = numBins;
     d.binCount = (int32_t*)(scratch + kOffBinCount);
     d.binStart = (int32_t*)(scratch + kOffBinStart);
     d.binUnitFirst = (int32_t*)(scratch + kOffBinUnitFirst);

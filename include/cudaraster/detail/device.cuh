@@ -71,7 +71,7 @@ struct InstanceDev {
     S32 tileBase;             // first global tile id
     S32 chunkBase;            // first global bin-stage chunk
     S32 numChunks;
-    S64 chunkCountBase;       // first entry of this instance in chunkBinCount
+    S64 chunkCountBase;       // first entry of this instance in chunkBinCount / chunkBinOffset
     S32 chunkTris;            // triangles per chunk
     S32 pipeGroup;            // index of the pipe this instance renders with
 };
@@ -84,6 +84,7 @@ struct Counters {
     S32 fineTile;             // fine-stage work counter
     S32 overflow;             // kOverflow* bits
     S32 coarseWork[2];        // coarse count / scatter unit counters (dynamic unit assignment)
+    S32 binWork[2];           // bin count / scatter chunk counters (dynamic chunk assignment)
     S32 binsDone;             // bin-scan CTAs finished (the last one plans the coarse units)
     S32 unitEntries;          // bin entries per coarse unit, as planned for this draw
 };
@@ -96,6 +97,7 @@ struct DrawDev {
     S32 totalBins;
     S32 totalTiles;
     S32 totalChunks;
+    S32 maxBins;              // bins of the largest instance
     S32 unitEntries;          // bin entries per coarse unit; <= 0: sized on the device from the bin entries
     S32 unitTarget;           // coarse units wanted when sized on the device (set by the launcher)
     S64 totalTris;
@@ -106,7 +108,8 @@ struct DrawDev {
     S32* subtriOwner;         // [maxSubtris - totalTris] triangle of an extra slot
     S64 maxSubtris;
     // bin
-    S32* chunkBinCount;       // per (chunk, bin): count, then exclusive offset
+    S32* chunkBinCount;       // per (bin, chunk): entry count; zero between draws (the bin scan clears it)
+    S32* chunkBinOffset;      // per (chunk, bin): exclusive offset of the chunk in the bin list
     S32* binCount;            // [totalBins]
     S32* binStart;            // [totalBins]
     S32* binUnitFirst;        // [totalBins]
