@@ -48,7 +48,8 @@ class DebugParams(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("bin_log2", C.c_int32), ("bin_chunk_tris", C.c_int32), ("coarse_unit_entries", C.c_int32),
-                ("fine_warps", C.c_int32), ("fine_ctas_per_sm", C.c_int32)]
+                ("fine_warps", C.c_int32), ("fine_ctas_per_sm", C.c_int32),
+                ("fine_self_pixels", C.c_int32)]
 
 
 class Instance(C.Structure):

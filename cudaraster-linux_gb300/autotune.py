@@ -23,6 +23,9 @@ sys.path.insert(0, str(HERE.parent))
 PKG = HERE.name
 
 
+SELF_PIXELS = (4, 6, 8, 10, 12, 16)
+
+
 def candidates(quick: bool = False):
     bins = (3, 4, 5)
     warps = (4, 8)
@@ -102,11 +105,20 @@ def main():
     cands = list(candidates(args.quick))
     for name in args.workloads.split(","):
         if name == "soup1m":
-            out[name] = tune_single(scenes.soup(1_000_000, 1920, 1080, seed=2), "PixelPipe_gouraud", cands)
+            scene = scenes.soup(1_000_000, 1920, 1080, seed=2)
+            run = lambda c: tune_single(scene, "PixelPipe_gouraud", c)  # noqa: E731
         elif name == "batch64":
-            out[name] = tune_batch(wl.Batch(scenes.batch(64, seed=4)), cands)
+            batch = wl.Batch(scenes.batch(64, seed=4))
+            run = lambda c: tune_batch(batch, c)  # noqa: E731
         else:
             raise SystemExit(f"unknown workload {name}")
+        res = run(cands)
+        if not args.quick:
+            # Second pass: the fine stage's self-rasterization threshold around the best grid point.
+            extra = run([dict(res["best"], fine_self_pixels=v) for v in SELF_PIXELS])
+            allc = sorted(res["candidates"] + extra["candidates"], key=lambda r: r["ms"])
+            res = {"best": allc[0]["tuning"], "ms": allc[0]["ms"], "candidates": allc}
+        out[name] = res
         print(name, out[name]["best"], out[name]["ms"], flush=True)
     Path(args.out).write_text(json.dumps(out, indent=1))
 

@@ -366,6 +366,8 @@ cr_status cr_set_tuning(cr_context* ctx, const cr_tuning* t) {
         return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaRaster: bin_log2 must be 3, 4 or 5");
     if (t->fine_warps > 0 && (t->fine_warps > 8 || (t->fine_warps & (t->fine_warps - 1))))
         return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaRaster: fine_warps must be 1, 2, 4 or 8");
+    if (t->fine_self_pixels < 0 || t->fine_self_pixels > 64)
+        return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaRaster: fine_self_pixels must be in [0, 64]");
     if (t->bin_chunk_tris > 0 && (t->bin_chunk_tris % 32))
         return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaRaster: bin_chunk_tris must be a multiple of 32");
     ctx->tuning = *t;
@@ -426,11 +428,15 @@ cr_status buildPlan(cr_context* ctx, const std::vector<HostInstance>& in, Plan& 
             if (h.pipe == p) plan.inst.push_back(h);
     const int side = 1 << plan.binLog2;
     // Bin chunks are taken by warps, in order: about 80 per SM (two per
-    // resident bin warp), of 256 to 65536 triangles.
+    // resident bin warp), of at most 65536 triangles and at least 256 (fewer,
+    // down to 32, for draws under 128K triangles, whose chunks would
+    // otherwise be too few to keep the warps busy), a multiple of 32.
     int64_t allTris = 0;
     for (const HostInstance& h : plan.inst) allTris += h.dev.numTris;
     const int64_t wantChunks = std::max<int64_t>(1, (int64_t)ctx->numSMs * 80);
-    const int autoChunk = (int)std::min<int64_t>(std::max<int64_t>((allTris + wantChunks - 1) / wantChunks, 256), 65536);
+    const int64_t floorChunk = std::min<int64_t>(256, std::max<int64_t>(32, allTris / 512));
+    int64_t chunk = std::min<int64_t>(std::max<int64_t>((allTris + wantChunks - 1) / wantChunks, floorChunk), 65536);
+    const int autoChunk = (int)((chunk + 31) & ~(int64_t)31);
     int64_t tri = 0;
     int32_t bins = 0, tiles = 0, chunks = 0;
     int64_t countBase = 0;
@@ -565,6 +571,7 @@ DrawDev makeDrawDev(cr_context* ctx, const Plan& plan) {
     d.chunkBinCount = ctx->chunkBinCount.as<int32_t>();
     d.chunkBinOffset = ctx->chunkBinOffset.as<int32_t>();
     d.maxBins = plan.maxBins;
+    d.fineSelfPixels = ctx->tuning.fine_self_pixels;
     d.binCount = ctx->binCount.as<int32_t>();
     d.binStart = ctx->binStart.as<int32_t>();
     d.binUnitFirst = ctx->binUnitFirst.as<int32_t>();

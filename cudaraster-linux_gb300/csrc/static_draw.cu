@@ -214,6 +214,7 @@ extern "C" cr_status cr_draw_triangles_static(const char* pipe_name, void* color
     d.chunkBinCount = (int32_t*)(scratch + kOffChunkCount);   // zero at load; each bin scan clears it again
     d.chunkBinOffset = (int32_t*)(scratch + kOffChunkOffset);
     d.maxBins = numBins;
+    d.fineSelfPixels = 0;
     d.binCount = (int32_t*)(scratch + kOffBinCount);
     d.binStart = (int32_t*)(scratch + kOffBinStart);
     d.binUnitFirst = (int32_t*)(scratch + kOffBinUnitFirst);

@@ -226,9 +226,10 @@ class CudaRaster:
         self._ib = buf
         self._check(self._lib.cr_set_index_buffer(self._ctx, ptr, int(ofs), int(numTris)))
 
-    def setTuning(self, bin_log2=0, bin_chunk_tris=0, coarse_unit_entries=0, fine_warps=0, fine_ctas_per_sm=0):
+    def setTuning(self, bin_log2=0, bin_chunk_tris=0, coarse_unit_entries=0, fine_warps=0, fine_ctas_per_sm=0,
+                  fine_self_pixels=0):
         self._need_init()
-        t = _lib.Tuning(bin_log2, bin_chunk_tris, coarse_unit_entries, fine_warps, fine_ctas_per_sm)
+        t = _lib.Tuning(bin_log2, bin_chunk_tris, coarse_unit_entries, fine_warps, fine_ctas_per_sm, fine_self_pixels)
         self._check(self._lib.cr_set_tuning(self._ctx, C.byref(t)))
 
     def setCapacity(self, max_subtris=0, max_bin_entries=0, max_tile_entries=0):

@@ -98,6 +98,7 @@ struct DrawDev {
     S32 totalTiles;
     S32 totalChunks;
     S32 maxBins;              // bins of the largest instance
+    S32 fineSelfPixels;       // fine stage: pixel-box size up to which a lane rasterizes a triangle alone
     S32 unitEntries;          // bin entries per coarse unit; <= 0: sized on the device from the bin entries
     S32 unitTarget;           // coarse units wanted when sized on the device (set by the launcher)
     S64 totalTris;

@@ -36,9 +36,11 @@
 namespace cr {
 
 constexpr int kFineMaxThreads = 256;
-// Triangles whose pixel box inside the tile has at most this many pixels get
-// their coverage from their own lane; larger ones from the whole warp.
-constexpr int kFineSelfPixels = 12;
+// Triangles whose pixel box inside the tile has at most DrawDev::fineSelfPixels
+// pixels get their coverage from their own lane; larger ones from the whole
+// warp. Defaults: 8 pixels at one sample, 12 with MSAA (more samples per pixel
+// make a lane's walk worth more).
+__host__ __device__ constexpr int fineSelfPixelsDefault(int samplesLog2) { return samplesLog2 == 0 ? 8 : 12; }
 
 
 template <int S>
@@ -218,6 +220,7 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
     const int lane = threadIdx.x & 31;
     const U32 ltMask = (1u << lane) - 1u;
     if (__ldg(&d.counters->overflow)) return;
+    const S32 selfPixels = d.fineSelfPixels > 0 ? d.fineSelfPixels : fineSelfPixelsDefault(S);
 
     for (;;) {
         S32 tile = 0;
@@ -289,15 +292,22 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
                 if (kDepth && (h.w & 0xFFFFF000u) >= tileZMax) valid = false;
                 if (valid) {
                     const TileEdges te = tileEdges(h, cx0, cy0);
-#pragma unroll
-                    for (int k = 0; k < 3; k++) {
-                        sm.E[k][lane] = te.E[k];
-                        sm.A[k][lane] = te.A[k];
-                        sm.B[k][lane] = te.B[k];
-                    }
                     const uint4* tdp = &d.triData[slot * 4];
                     uint4 q0 = __ldg(&tdp[0]);
-                    sm.td[0][lane] = q0.x; sm.td[1][lane] = q0.y; sm.td[2][lane] = q0.z; sm.td[3][lane] = q0.w;
+                    S32 bx0, bx1, by0, by1;
+                    const bool inTile = pixelBox<S>(te, bx0, bx1, by0, by1);
+                    self = !inTile || (bx1 - bx0 + 1) * (by1 - by0 + 1) <= selfPixels;
+                    // The visibility path reads a triangle's words from shared
+                    // memory only when the whole warp rasterizes it.
+                    if (!kVisibility || !self) {
+#pragma unroll
+                        for (int k = 0; k < 3; k++) {
+                            sm.E[k][lane] = te.E[k];
+                            sm.A[k][lane] = te.A[k];
+                            sm.B[k][lane] = te.B[k];
+                        }
+                        sm.td[0][lane] = q0.x; sm.td[1][lane] = q0.y; sm.td[2][lane] = q0.z; sm.td[3][lane] = q0.w;
+                    }
                     if constexpr (!kVisibility) {
                         uint4 q1 = __ldg(&tdp[1]), q2 = __ldg(&tdp[2]), q3 = __ldg(&tdp[3]);
                         sm.td[4][lane] = q1.x; sm.td[5][lane] = q1.y; sm.td[6][lane] = q1.z; sm.td[7][lane] = q1.w;
@@ -305,11 +315,8 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
                         sm.td[12][lane] = q3.x; sm.td[13][lane] = q3.y; sm.td[14][lane] = q3.z; sm.td[15][lane] = q3.w;
                         sm.tri[lane] = (S32)((S64)tri - triBase);
                     }
-                    S32 bx0, bx1, by0, by1;
-                    if (!pixelBox<S>(te, bx0, bx1, by0, by1)) {
-                        self = true;  // no pixel of the tile can be covered
-                    } else if ((bx1 - bx0 + 1) * (by1 - by0 + 1) <= kFineSelfPixels) {
-                        self = true;
+                    // No pixel of the tile can be covered (!inTile): nothing to do.
+                    if (inTile && self) {
                         const U32 order = (U32)(batch + lane + 1);
                         for (S32 py = by0; py <= by1; py++) {
                             for (S32 px = bx0; px <= bx1; px++) {

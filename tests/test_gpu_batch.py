@@ -92,6 +92,7 @@ def test_batch_graph_replays(cuda):
 
 
 TUNINGS = [dict(bin_log2=3), dict(bin_log2=5), dict(fine_warps=2), dict(fine_warps=4, fine_ctas_per_sm=1),
+           dict(fine_self_pixels=1), dict(fine_self_pixels=64),
            dict(bin_chunk_tris=96, coarse_unit_entries=64), dict(bin_chunk_tris=8192, coarse_unit_entries=4096),
            dict(bin_log2=3, fine_warps=8, bin_chunk_tris=1024, coarse_unit_entries=128)]
 
