@@ -274,7 +274,10 @@ def main():
     workloads = importlib.import_module(PKG + ".workloads")
     tuning = workloads.load_tuning("soup1m")
     if args.profile_frames > 0 and args.profile_workload != "soup1m":
-        print(json.dumps(workloads.profile_frames(args.profile_workload, args.profile_frames, tuning)))
+        wname = "flythrough" if args.profile_workload.startswith("flythrough") or args.profile_workload == "predicted" \
+            else args.profile_workload
+        print(json.dumps(workloads.profile_frames(args.profile_workload, args.profile_frames,
+                                                  workloads.load_tuning(wname))))
         return
     cr = pkg.CudaRaster()
     cr.init()
@@ -433,11 +436,11 @@ def main():
                                         "plain = 64 sequential drawTriangles, batched = one CUDA-graph replay")
     sub = None
     if rank == 0 and not args.no_subpixel:
-        sub = workloads.measure_subpixel(tuning=tuning)
+        sub = workloads.measure_subpixel(tuning=workloads.load_tuning("subpixel"))
         line["subpixel_stress"] = sub[0]
     fly = None
     if rank == 0 and not args.no_flythrough:
-        fly = workloads.measure_flythrough(tuning=tuning, keep=(FLY_ORACLE_FRAME,))
+        fly = workloads.measure_flythrough(tuning=workloads.load_tuning("flythrough"), keep=(FLY_ORACLE_FRAME,))
         line["flythrough"] = fly[0]
     if rank == 0 and not args.no_cpu_baseline:
         cb, (rc, rd, st) = cpu_baseline(sc)
