@@ -23,7 +23,7 @@ sys.path.insert(0, str(HERE.parent))
 PKG = HERE.name
 
 
-SELF_PIXELS = (4, 6, 8, 10, 12, 16)
+SELF_PIXELS = (4, 8, 12, 16, 24, 32, 48, 64)
 
 
 def candidates(quick: bool = False):

@@ -37,10 +37,15 @@ namespace cr {
 
 constexpr int kFineMaxThreads = 256;
 // Triangles whose pixel box inside the tile has at most DrawDev::fineSelfPixels
-// pixels get their coverage from their own lane; larger ones from the whole
-// warp. Defaults: 8 pixels at one sample, 12 with MSAA (more samples per pixel
-// make a lane's walk worth more).
-__host__ __device__ constexpr int fineSelfPixelsDefault(int samplesLog2) { return samplesLog2 == 0 ? 8 : 12; }
+// pixels are rasterized pixel by pixel by the lanes -- in the visibility path
+// their (triangle, pixel) pairs are dealt over all lanes, in the ordered path
+// one lane walks its own triangle's box; larger ones by the whole warp, two
+// pixels per lane. Defaults: 16 pixels in the visibility path; in the ordered
+// path 8 at one sample and 12 with MSAA (more samples per pixel make a lane's
+// walk worth more).
+__host__ __device__ constexpr int fineSelfPixelsDefault(int samplesLog2, bool visibility) {
+    return visibility ? 16 : (samplesLog2 == 0 ? 8 : 12);
+}
 
 
 template <int S>
@@ -220,7 +225,7 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
     const int lane = threadIdx.x & 31;
     const U32 ltMask = (1u << lane) - 1u;
     if (__ldg(&d.counters->overflow)) return;
-    const S32 selfPixels = d.fineSelfPixels > 0 ? d.fineSelfPixels : fineSelfPixelsDefault(S);
+    const S32 selfPixels = d.fineSelfPixels > 0 ? d.fineSelfPixels : fineSelfPixelsDefault(S, kVisibility);
 
     for (;;) {
         S32 tile = 0;
@@ -280,6 +285,125 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
         }
 
         for (S32 batch = 0; batch < count; batch += 32) {
+            if constexpr (kVisibility) {
+                // ---- Visibility. Every (triangle, pixel) pair of the batch's
+                // triangles whose pixel box has at most selfPixels pixels is
+                // dealt to the lanes in turn (pair p of the batch: its
+                // triangle j by a search over the prefix of box sizes, its
+                // pixel by an exact multiply-shift division by the box width;
+                // a lane walking its own triangle's box measured slower, even
+                // for boxes of one or two pixels); larger triangles are
+                // rasterized by the whole warp, two pixels per lane. Keys
+                // resolve by atomic minimum, so the order pairs are taken in
+                // does not change a bit.
+                S32 n = 0;
+                bool big = false;
+                if (batch + lane < count) {
+                    const U32 entry = __ldg(&d.tileList[start + batch + lane]);
+                    const U32 tri = entry >> 3, sub = entry & 7;
+                    const S64 slot = (sub == 7) ? (S64)tri : (S64)__ldg(&d.triHeader[tri].w) + sub;
+                    const uint4 h = __ldg(&d.triHeader[slot]);
+                    if ((h.w & 0xFFFFF000u) < tileZMax) {
+                        const TileEdges te = tileEdges(h, cx0, cy0);
+                        S32 bx0, bx1, by0, by1;
+                        if (pixelBox<S>(te, bx0, bx1, by0, by1)) {
+                            const uint4 q0 = __ldg(&d.triData[slot * 4]);
+                            const S32 w = bx1 - bx0 + 1;
+                            const S32 cnt = w * (by1 - by0 + 1);
+                            big = cnt > selfPixels;
+#pragma unroll
+                            for (int k = 0; k < 3; k++) {
+                                sm.E[k][lane] = te.E[k];
+                                sm.A[k][lane] = te.A[k];
+                                sm.B[k][lane] = te.B[k];
+                            }
+                            sm.td[0][lane] = q0.x;
+                            sm.td[1][lane] = q0.y;
+                            sm.td[2][lane] = q0.z;
+                            if (!big) {
+                                n = cnt;
+                                sm.covLo[lane] = (U32)bx0 | (U32)by0 << 4 | (U32)w << 8;
+                                // Row of box pixel k: (k * ceil(2^16 / w)) >> 16, exact for k < 64, w <= 8.
+                                sm.covHi[lane] = (65536u + (U32)w - 1u) / (U32)w;
+                            }
+                        }
+                    }
+                }
+                S32 P = 0;
+                if (__any_sync(0xFFFFFFFFu, n > 0)) {
+                    S32 incl = n;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const S32 t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                        if (lane >= o) incl += t;
+                    }
+                    sm.fragEnd[lane] = incl;
+                    P = __shfl_sync(0xFFFFFFFFu, incl, 31);
+                }
+                __syncwarp();
+                for (S32 base = 0; base < P; base += 32) {
+                    const S32 p = base + lane;
+                    if (p >= P) continue;
+                    int j = 0;
+#pragma unroll
+                    for (int s2 = 16; s2 > 0; s2 >>= 1)
+                        if (sm.fragEnd[j + s2 - 1] <= p) j += s2;
+                    const S32 k = p - (j ? sm.fragEnd[j - 1] : 0);
+                    const U32 bw = sm.covLo[j];
+                    const S32 w = (S32)(bw >> 8);
+                    const S32 q = (S32)(((U32)k * sm.covHi[j]) >> 16);
+                    const S32 px = (S32)(bw & 0xFu) + k - q * w, py = (S32)((bw >> 4) & 0xFu) + q;
+                    const S32 E[3] = {sm.E[0][j], sm.E[1][j], sm.E[2][j]};
+                    const S32 A[3] = {sm.A[0][j], sm.A[1][j], sm.A[2][j]};
+                    const S32 B[3] = {sm.B[0][j], sm.B[1][j], sm.B[2][j]};
+                    const U32 smask = sampleMaskOf<S>(E, A, B, px, py);
+                    if (!smask) continue;
+                    const U32 order = (U32)(batch + j + 1);
+                    const U64 low = packed ? (order << 8 | smask) : order;
+                    const U32 X = (U32)(tx * 8 + px), Y = (U32)(ty * 8 + py);
+                    const U32 zx = sm.td[0][j], zy = sm.td[1][j], zb = sm.td[2][j];
+#pragma unroll
+                    for (int i = 0; i < NS; i++) {
+                        if (!(smask >> i & 1)) continue;
+                        const int idx = py * 8 * NS + i * 8 + px;
+                        const U64 key = ((U64)sampleDepth<S>(zx, zy, zb, X, Y, i) << 32) | low;
+                        if (key < sm.key[idx]) atomicMin((unsigned long long*)&sm.key[idx], (unsigned long long)key);
+                    }
+                }
+                __syncwarp();
+                // Larger triangles: the whole warp, one at a time (each lane
+                // owns its two pixels, so plain stores suffice).
+                const S32 px = lane & 7, py0 = lane >> 3, py1 = py0 + 4;
+                const U32 pX = (U32)(tx * 8 + px), pY0 = (U32)(ty * 8 + py0), pY1 = pY0 + 4;
+                for (U32 m = __ballot_sync(0xFFFFFFFFu, big); m; m &= m - 1) {
+                    const int j = __ffs(m) - 1;
+                    const S32 E[3] = {sm.E[0][j], sm.E[1][j], sm.E[2][j]};
+                    const S32 A[3] = {sm.A[0][j], sm.A[1][j], sm.A[2][j]};
+                    const S32 B[3] = {sm.B[0][j], sm.B[1][j], sm.B[2][j]};
+                    const U32 zx = sm.td[0][j], zy = sm.td[1][j], zb = sm.td[2][j];
+                    const U32 order = (U32)(batch + j + 1);
+#pragma unroll
+                    for (int half = 0; half < 2; half++) {
+                        const S32 pyy = half ? py1 : py0;
+                        const U32 Y = half ? pY1 : pY0;
+                        const U32 smask = sampleMaskOf<S>(E, A, B, px, pyy);
+                        const U64 low = packed ? (order << 8 | smask) : order;
+#pragma unroll
+                        for (int i = 0; i < NS; i++) {
+                            if (!(smask >> i & 1)) continue;
+                            const int idx = pyy * 8 * NS + i * 8 + px;
+                            const U64 key = ((U64)sampleDepth<S>(zx, zy, zb, pX, Y, i) << 32) | low;
+                            if (key < sm.key[idx]) sm.key[idx] = key;
+                        }
+                    }
+                }
+                __syncwarp();
+                // Exact current depth maximum for the next batch's early Z.
+                U32 z = 0;
+                for (int w = lane; w < TW; w += 32) z = max(z, (U32)(sm.key[w] >> 32));
+                tileZMax = __reduce_max_sync(0xFFFFFFFFu, z);
+                continue;
+            }
             // ---- 1. One triangle per lane.
             bool valid = batch + lane < count;
             bool self = false;     // small triangle: this lane handles all of it
@@ -297,41 +421,25 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
                     S32 bx0, bx1, by0, by1;
                     const bool inTile = pixelBox<S>(te, bx0, bx1, by0, by1);
                     self = !inTile || (bx1 - bx0 + 1) * (by1 - by0 + 1) <= selfPixels;
-                    // The visibility path reads a triangle's words from shared
-                    // memory only when the whole warp rasterizes it.
-                    if (!kVisibility || !self) {
 #pragma unroll
-                        for (int k = 0; k < 3; k++) {
-                            sm.E[k][lane] = te.E[k];
-                            sm.A[k][lane] = te.A[k];
-                            sm.B[k][lane] = te.B[k];
-                        }
-                        sm.td[0][lane] = q0.x; sm.td[1][lane] = q0.y; sm.td[2][lane] = q0.z; sm.td[3][lane] = q0.w;
+                    for (int k = 0; k < 3; k++) {
+                        sm.E[k][lane] = te.E[k];
+                        sm.A[k][lane] = te.A[k];
+                        sm.B[k][lane] = te.B[k];
                     }
-                    if constexpr (!kVisibility) {
-                        uint4 q1 = __ldg(&tdp[1]), q2 = __ldg(&tdp[2]), q3 = __ldg(&tdp[3]);
-                        sm.td[4][lane] = q1.x; sm.td[5][lane] = q1.y; sm.td[6][lane] = q1.z; sm.td[7][lane] = q1.w;
-                        sm.td[8][lane] = q2.x; sm.td[9][lane] = q2.y; sm.td[10][lane] = q2.z; sm.td[11][lane] = q2.w;
-                        sm.td[12][lane] = q3.x; sm.td[13][lane] = q3.y; sm.td[14][lane] = q3.z; sm.td[15][lane] = q3.w;
-                        sm.tri[lane] = (S32)((S64)tri - triBase);
-                    }
+                    sm.td[0][lane] = q0.x; sm.td[1][lane] = q0.y; sm.td[2][lane] = q0.z; sm.td[3][lane] = q0.w;
+                    uint4 q1 = __ldg(&tdp[1]), q2 = __ldg(&tdp[2]), q3 = __ldg(&tdp[3]);
+                    sm.td[4][lane] = q1.x; sm.td[5][lane] = q1.y; sm.td[6][lane] = q1.z; sm.td[7][lane] = q1.w;
+                    sm.td[8][lane] = q2.x; sm.td[9][lane] = q2.y; sm.td[10][lane] = q2.z; sm.td[11][lane] = q2.w;
+                    sm.td[12][lane] = q3.x; sm.td[13][lane] = q3.y; sm.td[14][lane] = q3.z; sm.td[15][lane] = q3.w;
+                    sm.tri[lane] = (S32)((S64)tri - triBase);
                     // No pixel of the tile can be covered (!inTile): nothing to do.
                     if (inTile && self) {
                         const U32 order = (U32)(batch + lane + 1);
                         for (S32 py = by0; py <= by1; py++) {
                             for (S32 px = bx0; px <= bx1; px++) {
                                 const U32 X = (U32)(tx * 8 + px), Y = (U32)(ty * 8 + py);
-                                if constexpr (kVisibility) {
-                                    const U32 smask = sampleMaskOf<S>(te.E, te.A, te.B, px, py);
-                                    const U64 low = packed ? (order << 8 | smask) : order;
-#pragma unroll
-                                    for (int i = 0; i < NS; i++) {
-                                        if (!(smask >> i & 1)) continue;
-                                        const int idx = py * 8 * NS + i * 8 + px;
-                                        const U64 k = ((U64)sampleDepth<S>(q0.x, q0.y, q0.z, X, Y, i) << 32) | low;
-                                        if (k < sm.key[idx]) atomicMin((unsigned long long*)&sm.key[idx], (unsigned long long)k);
-                                    }
-                                } else {
+                                {
                                     const S32 qx = px << kSubpixelLog2, qy = py << kSubpixelLog2;
                                     bool c = true;
 #pragma unroll
@@ -356,36 +464,7 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
             // ---- 2. Large triangles, two pixels per lane.
             const S32 px = lane & 7, py0 = lane >> 3, py1 = py0 + 4;
             const U32 pX = (U32)(tx * 8 + px), pY0 = (U32)(ty * 8 + py0), pY1 = pY0 + 4;
-            if constexpr (kVisibility) {
-                for (U32 m = coopMask; m; m &= m - 1) {
-                    const int j = __ffs(m) - 1;
-                    const S32 E[3] = {sm.E[0][j], sm.E[1][j], sm.E[2][j]};
-                    const S32 A[3] = {sm.A[0][j], sm.A[1][j], sm.A[2][j]};
-                    const S32 B[3] = {sm.B[0][j], sm.B[1][j], sm.B[2][j]};
-                    const U32 zx = sm.td[0][j], zy = sm.td[1][j], zb = sm.td[2][j];
-                    const U32 order = (U32)(batch + j + 1);
-#pragma unroll
-                    for (int half = 0; half < 2; half++) {
-                        const S32 pyy = half ? py1 : py0;
-                        const U32 Y = half ? pY1 : pY0;
-                        const U32 smask = sampleMaskOf<S>(E, A, B, px, pyy);
-                        const U64 low = packed ? (order << 8 | smask) : order;
-#pragma unroll
-                        for (int i = 0; i < NS; i++) {
-                            if (!(smask >> i & 1)) continue;
-                            const int idx = pyy * 8 * NS + i * 8 + px;
-                            const U64 k = ((U64)sampleDepth<S>(zx, zy, zb, pX, Y, i) << 32) | low;
-                            if (k < sm.key[idx]) sm.key[idx] = k;
-                        }
-                    }
-                }
-                __syncwarp();
-                // Exact current depth maximum for the next batch's early Z.
-                U32 z = 0;
-                for (int w = lane; w < TW; w += 32) z = max(z, (U32)(sm.key[w] >> 32));
-                tileZMax = __reduce_max_sync(0xFFFFFFFFu, z);
-                continue;
-            } else {
+            {
                 // Single-sample depth of this lane's two pixels at the start of
                 // the batch: a fragment that fails against it fails in
                 // submission order too (depths only decrease).
