@@ -625,81 +625,100 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
         }
 
         if constexpr (kVisibility) {
-            // ---- Resolve: shade every (pixel, winning triangle) once. A lane
-            // owns pixels lane and lane + 32; sample i0 of a pixel starts a
-            // winner if no earlier sample of the pixel has the same key low
-            // word (with MSAA the low word carries the winner's coverage mask,
-            // so neither its edges nor its mask are recomputed here).
-#pragma unroll 1
-            for (int i0 = 0; i0 < NS; i0++) {
-                U32 low[2], won[2], tri[2], td[2][16];
-                auto fetch = [&](int h) {
-                    const int p = lane + 32 * h;
-                    const int rowBase = (p >> 3) * 8 * NS + (p & 7);
-                    low[h] = (U32)sm.key[rowBase + i0 * 8];
-                    won[h] = 0;
-                    if (low[h] != 0) {
-                        bool first = true;
-                        for (int i = 0; i < i0; i++)
-                            if ((U32)sm.key[rowBase + i * 8] == low[h]) first = false;
-                        if (first)
+            // ---- Resolve: shade every (pixel, winning triangle) once. Sample
+            // i0 of a pixel starts a winner if no earlier sample of the pixel
+            // has the same key low word (with MSAA the low word carries the
+            // winner's coverage mask, so neither its edges nor its mask are
+            // recomputed here). The winners of the tile are listed first (a
+            // lane owns pixels lane and lane + 32), then fetched and shaded
+            // 32 at a time, so lanes stay busy however unevenly the winners
+            // fall on the pixels and samples.
+            // Winner records (pixel | first sample << 6 | samples won << 9), at
+            // most 64 << S <= 512 of them, in the triangle words (free by now).
+            U32* winners = &sm.td[0][0];
+            S32 nw = 0;
 #pragma unroll
-                            for (int i = 0; i < NS; i++)
-                                if ((U32)sm.key[rowBase + i * 8] == low[h]) won[h] |= 1u << i;
-                    }
-                    tri[h] = 0;
-                    if (won[h]) {
-                        const U32 entry = __ldg(&d.tileList[start + (S32)(packed ? (low[h] >> 8) : low[h]) - 1]);
-                        const U32 sub = entry & 7;
-                        tri[h] = entry >> 3;
-                        const S64 slot = (sub == 7) ? (S64)tri[h] : (S64)__ldg(&d.triHeader[tri[h]].w) + sub;
-                        const uint4* tdp = &d.triData[slot * 4];
-                        const uint4 q1 = __ldg(&tdp[1]), q2 = __ldg(&tdp[2]), q3 = __ldg(&tdp[3]);
-                        td[h][4] = q1.x; td[h][5] = q1.y; td[h][6] = q1.z; td[h][7] = q1.w;
-                        td[h][8] = q2.x; td[h][9] = q2.y; td[h][10] = q2.z; td[h][11] = q2.w;
-                        td[h][12] = q3.x; td[h][13] = q3.y; td[h][14] = q3.z; td[h][15] = q3.w;
-                        if (S != 0 && !packed) {
-                            const TileEdges te = tileEdges(__ldg(&d.triHeader[slot]), cx0, cy0);
-                            low[h] = sampleMaskOf<S>(te.E, te.A, te.B, p & 7, p >> 3);
-                        } else if (S != 0) {
-                            low[h] &= 0xFFu;
-                        }
-                    }
-                };
-                auto shade = [&](int h) {
-                    if (!won[h]) return;
-                    const int p = lane + 32 * h;
-                    const S32 px = p & 7, py = p >> 3;
-                    const int rowBase = py * 8 * NS + px;
-                    bool discard;
-                    const S32 X = tx * 8 + px, Y = ty * 8 + py;
-                    const S32 triIdx = (S32)((S64)tri[h] - triBase);
-                    // low[h] now holds the winner's coverage mask of the pixel (MSAA).
-                    const U32 src = shadeFragment<FS, S, F>(td[h], triIdx, X, Y, S != 0 ? low[h] : 1u, verts, stride4,
-                                                            sm.shared, 0u, discard);
-                    BS bs;
+            for (int hh = 0; hh < 2; hh++) {
+                const int p = lane + 32 * hh;
+                const int rowBase = (p >> 3) * 8 * NS + (p & 7);
+                U32 mine[NS];
+                int cnt = 0;
 #pragma unroll
-                    for (int i = 0; i < NS; i++) {
-                        if (!(won[h] >> i & 1)) continue;
-                        const int idx = rowBase + i * 8;
-                        sm.depth[idx] = (U32)(sm.key[idx] >> 32);
-                        bs.m_triIdx = triIdx;
-                        bs.m_pixelPos = FW::Vec2i(X, Y);
-                        bs.m_sampleIdx = i;
-                        bs.m_src = src;
-                        bs.m_dst = sm.color[idx];
-                        bs.m_color = 0xFF0000FFu;
-                        bs.m_writeColor = true;
-                        bs.run();
-                        if (bs.m_writeColor) sm.color[idx] = bs.m_color;
+                for (int i0 = 0; i0 < NS; i0++) {
+                    const U32 low = (U32)sm.key[rowBase + i0 * 8];
+                    bool first = low != 0;
+#pragma unroll
+                    for (int i = 0; i < i0; i++)
+                        if ((U32)sm.key[rowBase + i * 8] == low) first = false;
+                    U32 won = 0;
+                    if (first) {
+#pragma unroll
+                        for (int i = 0; i < NS; i++)
+                            if ((U32)sm.key[rowBase + i * 8] == low) won |= 1u << i;
                     }
-                };
-                // One pixel at a time: fetching both pixels' data before
-                // shading either measured slower (registers, occupancy).
-                fetch(0);
-                shade(0);
-                fetch(1);
-                shade(1);
+                    mine[i0] = (U32)p | (U32)i0 << 6 | won << 9;
+                    cnt += first ? 1 : 0;
+                }
+                S32 pos = cnt;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const S32 t = __shfl_up_sync(0xFFFFFFFFu, pos, o);
+                    if (lane >= o) pos += t;
+                }
+                const S32 total = __shfl_sync(0xFFFFFFFFu, pos, 31);
+                pos += nw - cnt;
+#pragma unroll
+                for (int i0 = 0; i0 < NS; i0++)
+                    if (mine[i0] >> 9) winners[pos++] = mine[i0];
+                nw += total;
+            }
+            __syncwarp();
+            for (S32 w0 = 0; w0 < nw; w0 += 32) {
+                if (w0 + lane >= nw) continue;
+                const U32 rec = winners[w0 + lane];
+                const int p = (int)(rec & 63u), i0 = (int)((rec >> 6) & 7u);
+                const U32 won = rec >> 9;
+                const S32 px = p & 7, py = p >> 3;
+                const int rowBase = py * 8 * NS + px;
+                U32 low = (U32)sm.key[rowBase + i0 * 8];
+                U32 td[16];
+                const U32 entry = __ldg(&d.tileList[start + (S32)(packed ? (low >> 8) : low) - 1]);
+                const U32 sub = entry & 7;
+                const U32 tri = entry >> 3;
+                const S64 slot = (sub == 7) ? (S64)tri : (S64)__ldg(&d.triHeader[tri].w) + sub;
+                const uint4* tdp = &d.triData[slot * 4];
+                const uint4 q1 = __ldg(&tdp[1]), q2 = __ldg(&tdp[2]), q3 = __ldg(&tdp[3]);
+                td[4] = q1.x; td[5] = q1.y; td[6] = q1.z; td[7] = q1.w;
+                td[8] = q2.x; td[9] = q2.y; td[10] = q2.z; td[11] = q2.w;
+                td[12] = q3.x; td[13] = q3.y; td[14] = q3.z; td[15] = q3.w;
+                if (S != 0 && !packed) {
+                    const TileEdges te = tileEdges(__ldg(&d.triHeader[slot]), cx0, cy0);
+                    low = sampleMaskOf<S>(te.E, te.A, te.B, px, py);
+                } else if (S != 0) {
+                    low &= 0xFFu;
+                }
+                bool discard;
+                const S32 X = tx * 8 + px, Y = ty * 8 + py;
+                const S32 triIdx = (S32)((S64)tri - triBase);
+                // low now holds the winner's coverage mask of the pixel (MSAA).
+                const U32 src = shadeFragment<FS, S, F>(td, triIdx, X, Y, S != 0 ? low : 1u, verts, stride4,
+                                                        sm.shared, 0u, discard);
+                BS bs;
+#pragma unroll
+                for (int i = 0; i < NS; i++) {
+                    if (!(won >> i & 1)) continue;
+                    const int idx = rowBase + i * 8;
+                    sm.depth[idx] = (U32)(sm.key[idx] >> 32);
+                    bs.m_triIdx = triIdx;
+                    bs.m_pixelPos = FW::Vec2i(X, Y);
+                    bs.m_sampleIdx = i;
+                    bs.m_src = src;
+                    bs.m_dst = sm.color[idx];
+                    bs.m_color = 0xFF0000FFu;
+                    bs.m_writeColor = true;
+                    bs.run();
+                    if (bs.m_writeColor) sm.color[idx] = bs.m_color;
+                }
             }
             __syncwarp();
         }
