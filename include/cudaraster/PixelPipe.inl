@@ -55,13 +55,18 @@ struct PipeImpl {
         kern<<<(unsigned)grid, warps * 32, smemBytes(warps), stream>>>(d, group, tileBegin, tileEnd);
         return cudaGetLastError();
     }
+    // Resident fine CTAs per SM, by warps per CTA (queried once per size).
     static int fineOccupancy(int warps) {
+        static int cache[9] = {};
+        const int w = warps >= 1 && warps <= 8 ? warps : 8;
+        if (cache[w] > 0) return cache[w];
         auto kern = fineKernel<V, FS, BS, S, F>;
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
         int blocks = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, warps * 32, smemBytes(warps)) != cudaSuccess)
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, w * 32, smemBytes(w)) != cudaSuccess)
             return 1;
-        return blocks > 0 ? blocks : 1;
+        cache[w] = blocks > 0 ? blocks : 1;
+        return cache[w];
     }
     static void describe(PipeDesc& p, const char* name, const char* blend, const char* frag) {
         memset(&p, 0, sizeof(p));
