@@ -119,8 +119,7 @@ typedef struct cr_tuning {
     int32_t fine_self_pixels;     /* fine stage: triangles whose pixel box in a tile  */
                                   /* has at most this many pixels are rasterized      */
                                   /* pixel by pixel by the lanes, larger ones by the  */
-                                  /* whole warp (default 16 for opaque depth-tested   */
-                                  /* pipes; 8 at 1 spp and 12 with MSAA otherwise)    */
+                                  /* whole warp (default 16)                          */
 } cr_tuning;
 
 /* One scene of a batched draw (cr_draw_batch). All pointers are device pointers. */

@@ -37,15 +37,10 @@ namespace cr {
 
 constexpr int kFineMaxThreads = 256;
 // Triangles whose pixel box inside the tile has at most DrawDev::fineSelfPixels
-// pixels are rasterized pixel by pixel by the lanes -- in the visibility path
-// their (triangle, pixel) pairs are dealt over all lanes, in the ordered path
-// one lane walks its own triangle's box; larger ones by the whole warp, two
-// pixels per lane. Defaults: 16 pixels in the visibility path; in the ordered
-// path 8 at one sample and 12 with MSAA (more samples per pixel make a lane's
-// walk worth more).
-__host__ __device__ constexpr int fineSelfPixelsDefault(int samplesLog2, bool visibility) {
-    return visibility ? 16 : (samplesLog2 == 0 ? 8 : 12);
-}
+// pixels are rasterized pixel by pixel by the lanes -- their (triangle, pixel)
+// pairs are dealt over all lanes; larger ones by the whole warp, two
+// pixels per lane. Default: 16 pixels.
+__host__ __device__ constexpr int fineSelfPixelsDefault(int, bool) { return 16; }
 
 
 template <int S>
@@ -404,10 +399,19 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
                 tileZMax = __reduce_max_sync(0xFFFFFFFFu, z);
                 continue;
             }
-            // ---- 1. One triangle per lane.
+            // ---- 1. One triangle per lane: its words in shared memory, and
+            // the pixels of the small ones (box of at most selfPixels pixels)
+            // as (triangle, pixel) pairs dealt over the lanes, each setting
+            // the triangle's coverage bit of its pixel (the masks do not
+            // depend on the order the pairs are taken in).
             bool valid = batch + lane < count;
-            bool self = false;     // small triangle: this lane handles all of it
+            bool self = false;     // small triangle: covered through the pairs
             U32 myLo = 0, myHi = 0;
+            S32 n = 0;
+            U32* pairBox = reinterpret_cast<U32*>(sm.key);        // [32] bx0 | by0 << 4 | w << 8
+            U32* pairMul = reinterpret_cast<U32*>(sm.key) + 32;   // [32] ceil(2^16 / w)
+            sm.covLo[lane] = 0u;
+            sm.covHi[lane] = 0u;
             if (valid) {
                 U32 entry = __ldg(&d.tileList[start + batch + lane]);
                 U32 tri = entry >> 3, sub = entry & 7;
@@ -420,7 +424,8 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
                     uint4 q0 = __ldg(&tdp[0]);
                     S32 bx0, bx1, by0, by1;
                     const bool inTile = pixelBox<S>(te, bx0, bx1, by0, by1);
-                    self = !inTile || (bx1 - bx0 + 1) * (by1 - by0 + 1) <= selfPixels;
+                    const S32 w = bx1 - bx0 + 1;
+                    self = !inTile || w * (by1 - by0 + 1) <= selfPixels;
 #pragma unroll
                     for (int k = 0; k < 3; k++) {
                         sm.E[k][lane] = te.E[k];
@@ -435,28 +440,58 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
                     sm.tri[lane] = (S32)((S64)tri - triBase);
                     // No pixel of the tile can be covered (!inTile): nothing to do.
                     if (inTile && self) {
-                        const U32 order = (U32)(batch + lane + 1);
-                        for (S32 py = by0; py <= by1; py++) {
-                            for (S32 px = bx0; px <= bx1; px++) {
-                                const U32 X = (U32)(tx * 8 + px), Y = (U32)(ty * 8 + py);
-                                {
-                                    const S32 qx = px << kSubpixelLog2, qy = py << kSubpixelLog2;
-                                    bool c = true;
-#pragma unroll
-                                    for (int k = 0; k < 3; k++) {
-                                        S32 slack = (S == 0) ? 0 : (abs(te.A[k]) + abs(te.B[k])) << (kSubpixelLog2 - 1);
-                                        c = c && (te.E[k] + te.A[k] * qx + te.B[k] * qy + slack >= 0);
-                                    }
-                                    if (kDepth && S == 0 && !kQuads && c) c = (q0.x * X + q0.y * Y + q0.z) < sm.depth[py * 8 + px];
-                                    if (c) {
-                                        const int bit = py * 8 + px;
-                                        if (bit < 32) myLo |= 1u << bit; else myHi |= 1u << (bit - 32);
-                                    }
-                                }
-                            }
-                        }
+                        n = w * (by1 - by0 + 1);
+                        pairBox[lane] = (U32)bx0 | (U32)by0 << 4 | (U32)w << 8;
+                        // Row of box pixel k: (k * ceil(2^16 / w)) >> 16, exact for k < 64, w <= 8.
+                        pairMul[lane] = (65536u + (U32)w - 1u) / (U32)w;
                     }
                 }
+            }
+            S32 P = 0;
+            if (__any_sync(0xFFFFFFFFu, n > 0)) {
+                S32 incl = n;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const S32 t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                    if (lane >= o) incl += t;
+                }
+                sm.fragEnd[lane] = incl;
+                P = __shfl_sync(0xFFFFFFFFu, incl, 31);
+            }
+            __syncwarp();
+            for (S32 base = 0; base < P; base += 32) {
+                const S32 p = base + lane;
+                if (p >= P) continue;
+                int j = 0;
+#pragma unroll
+                for (int s2 = 16; s2 > 0; s2 >>= 1)
+                    if (sm.fragEnd[j + s2 - 1] <= p) j += s2;
+                const S32 k = p - (j ? sm.fragEnd[j - 1] : 0);
+                const U32 bw = pairBox[j];
+                const S32 w = (S32)(bw >> 8);
+                const S32 q = (S32)(((U32)k * pairMul[j]) >> 16);
+                const S32 px = (S32)(bw & 0xFu) + k - q * w, py = (S32)((bw >> 4) & 0xFu) + q;
+                const S32 qx = px << kSubpixelLog2, qy = py << kSubpixelLog2;
+                bool c = true;
+#pragma unroll
+                for (int e = 0; e < 3; e++) {
+                    const S32 a = sm.A[e][j], b = sm.B[e][j];
+                    const S32 slack = (S == 0) ? 0 : (abs(a) + abs(b)) << (kSubpixelLog2 - 1);
+                    c = c && (sm.E[e][j] + a * qx + b * qy + slack >= 0);
+                }
+                if (kDepth && S == 0 && !kQuads && c) {
+                    const U32 X = (U32)(tx * 8 + px), Y = (U32)(ty * 8 + py);
+                    c = (sm.td[0][j] * X + sm.td[1][j] * Y + sm.td[2][j]) < sm.depth[py * 8 + px];
+                }
+                if (c) {
+                    const int bit = py * 8 + px;
+                    atomicOr(bit < 32 ? &sm.covLo[j] : &sm.covHi[j], 1u << (bit & 31));
+                }
+            }
+            __syncwarp();
+            if (self) {
+                myLo = sm.covLo[lane];
+                myHi = sm.covHi[lane];
             }
             __syncwarp();
             const U32 coopMask = __ballot_sync(0xFFFFFFFFu, valid && !self);
