@@ -37,11 +37,11 @@ struct PipeImpl {
         setupKernel<S, F & (kRenderDepth | kRenderLerp)><<<grid, 256, 0, stream>>>(d, instBegin, instEnd, triBegin, triEnd);
         return cudaGetLastError();
     }
-    static size_t smemBytes(int warps) { return sizeof(FineWarpSmem<S>) * (size_t)warps; }
+    static size_t smemBytes(int warps) { return sizeof(typename FineTraits<FS, BS, S, F>::Smem) * (size_t)warps; }
     static cudaError_t launchFine(const DrawDev& d, int group, int32_t tileBegin, int32_t tileEnd, int warps,
                                   int ctasPerSM, int numSMs, cudaStream_t stream) {
         if (tileEnd <= tileBegin) return cudaSuccess;
-        auto kern = fineKernel<V, FS, BS, S, F>;
+        auto kern = fineKernelFor<V, FS, BS, S, F>();
         static bool configured = false;
         if (!configured) {
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
@@ -60,7 +60,7 @@ struct PipeImpl {
         static int cache[9] = {};
         const int w = warps >= 1 && warps <= 8 ? warps : 8;
         if (cache[w] > 0) return cache[w];
-        auto kern = fineKernel<V, FS, BS, S, F>;
+        auto kern = fineKernelFor<V, FS, BS, S, F>();
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
         int blocks = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, w * 32, smemBytes(w)) != cudaSuccess)

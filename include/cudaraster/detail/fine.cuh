@@ -33,6 +33,8 @@
 #include "../PixelPipe.hpp"
 #include "device.cuh"
 
+#include <type_traits>
+
 namespace cr {
 
 constexpr int kFineMaxThreads = 256;
@@ -43,12 +45,14 @@ constexpr int kFineMaxThreads = 256;
 __host__ __device__ constexpr int fineSelfPixelsDefault(int, bool) { return 16; }
 
 
+// The ordered path's per-warp state (one warp per tile).
 template <int S>
 struct FineWarpSmem {
     static constexpr int kTileWords = 64 << S;
     U32 color[kTileWords];
     U32 depth[kTileWords];
-    U64 key[kTileWords];   // visibility keys (visibility path only)
+    U32 pairBox[32];       // bx0 | by0 << 4 | w << 8 of each small triangle's pixel box
+    U32 pairMul[32];       // ceil(2^16 / w)
     S32 E[3][32];          // edge functions at the tile's pixel (0, 0) centre, bias folded in
     S32 A[3][32];          // per-subpixel x step (-dy)
     S32 B[3][32];          // per-subpixel y step (+dx)
@@ -58,6 +62,35 @@ struct FineWarpSmem {
     U32 covHi[32];
     S32 fragEnd[32];
     F32 shared[32];
+};
+
+// The visibility path's per-warp state: no separate depth array (a key's high
+// word is its sample's depth) and only the triangle words it reads.
+template <int S>
+struct FineVisSmem {
+    static constexpr int kTileWords = 64 << S;
+    U32 color[kTileWords];
+    U64 key[kTileWords];        // depth << 32 | order (order << 8 | coverage mask with MSAA)
+    S32 E[3][32];
+    S32 A[3][32];
+    S32 B[3][32];
+    U32 z[3][32];               // depth plane (zx, zy, zb) of the batch's triangles
+    U32 box[32];                // bx0 | by0 << 4 | w << 8 of each small triangle's pixel box
+    U32 mul[32];                // ceil(2^16 / w)
+    S32 pairEnd[32];            // inclusive prefix of the pair counts
+    U32 winners[kTileWords];    // resolve: (pixel | first sample << 6 | samples won << 9)
+    F32 shared[32];
+};
+
+// Compile-time shape of a pipe's fine stage.
+template <class FS, class BS, int S, U32 F>
+struct FineTraits {
+    static constexpr bool kDepth = (F & kRenderDepth) != 0;
+    static constexpr bool kQuads = (F & kRenderQuads) != 0;
+    // Opaque depth-tested pipes resolve visibility with keys (see fineKernel).
+    static constexpr bool kVisibility = kDepth && !kQuads && !FW::BlendShaderTraits<BS>::needsDst &&
+                                        !FW::FragmentShaderTraits<FS>::mayDiscard;
+    using Smem = typename std::conditional<kVisibility, FineVisSmem<S>, FineWarpSmem<S>>::type;
 };
 
 __device__ __forceinline__ int nthSetBit32(U32 m, int n) {
@@ -208,15 +241,15 @@ __device__ __forceinline__ U32 shadeFragment(const U32* td, S32 triIdx, S32 X, S
 }
 
 template <class V, class FS, class BS, int S, U32 F>
-__global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int group, S32 tileBegin, S32 tileEnd) {
+__device__ __forceinline__ void fineTiles(const DrawDev& d, int group, S32 tileBegin, S32 tileEnd) {
     constexpr int NS = 1 << S;
     constexpr int TW = 64 << S;
-    constexpr bool kDepth = (F & kRenderDepth) != 0;
-    constexpr bool kQuads = (F & kRenderQuads) != 0;
-    constexpr bool kVisibility = kDepth && !kQuads && !FW::BlendShaderTraits<BS>::needsDst &&
-                                 !FW::FragmentShaderTraits<FS>::mayDiscard;
+    using Traits = FineTraits<FS, BS, S, F>;
+    constexpr bool kDepth = Traits::kDepth;
+    constexpr bool kQuads = Traits::kQuads;
+    constexpr bool kVisibility = Traits::kVisibility;
     extern __shared__ __align__(16) unsigned char fineSmemRaw[];
-    FineWarpSmem<S>& sm = reinterpret_cast<FineWarpSmem<S>*>(fineSmemRaw)[threadIdx.x >> 5];
+    typename Traits::Smem& sm = reinterpret_cast<typename Traits::Smem*>(fineSmemRaw)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     const U32 ltMask = (1u << lane) - 1u;
     if (__ldg(&d.counters->overflow)) return;
@@ -244,23 +277,44 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
         U32* gDepth = (U32*)__ldg((const unsigned long long*)&in->depth);
         const S64 tileOrigin = (S64)(ty * 8) * rowWords + (S64)tx * 8 * NS;
 
-        // Load or clear the tile (FineRaster.inl:562-580, 916-934).
-        if (clear) {
-            const U32 cc = __ldg(&in->clearColor), cd = __ldg(&in->clearDepth);
-            for (int w = lane; w < TW; w += 32) { sm.color[w] = cc; sm.depth[w] = cd; }
-        } else {
-            for (int w = lane; w < TW; w += 32) {
-                S64 g = tileOrigin + (S64)(w / (8 * NS)) * rowWords + (w % (8 * NS));
-                sm.color[w] = gColor[g];
-                sm.depth[w] = gDepth[g];
-            }
-        }
-        __syncwarp();
+        // Load or clear the tile (FineRaster.inl:562-580, 916-934), and its
+        // maximum depth for early Z.
         U32 tileZMax = 0;
-        if (kDepth) {
+        if constexpr (kVisibility) {
+            // Visibility keys start as depth << 32 (no fragment yet).
             U32 z = 0;
-            for (int w = lane; w < TW; w += 32) z = max(z, sm.depth[w]);
+            if (clear) {
+                const U32 cc = __ldg(&in->clearColor), cd = __ldg(&in->clearDepth);
+                for (int w = lane; w < TW; w += 32) { sm.color[w] = cc; sm.key[w] = (U64)cd << 32; }
+                z = cd;
+            } else {
+                for (int w = lane; w < TW; w += 32) {
+                    S64 g = tileOrigin + (S64)(w / (8 * NS)) * rowWords + (w % (8 * NS));
+                    sm.color[w] = gColor[g];
+                    const U32 dz = gDepth[g];
+                    sm.key[w] = (U64)dz << 32;
+                    z = max(z, dz);
+                }
+            }
             tileZMax = __reduce_max_sync(0xFFFFFFFFu, z);
+            __syncwarp();
+        } else {
+            if (clear) {
+                const U32 cc = __ldg(&in->clearColor), cd = __ldg(&in->clearDepth);
+                for (int w = lane; w < TW; w += 32) { sm.color[w] = cc; sm.depth[w] = cd; }
+            } else {
+                for (int w = lane; w < TW; w += 32) {
+                    S64 g = tileOrigin + (S64)(w / (8 * NS)) * rowWords + (w % (8 * NS));
+                    sm.color[w] = gColor[g];
+                    sm.depth[w] = gDepth[g];
+                }
+            }
+            __syncwarp();
+            if (kDepth) {
+                U32 z = 0;
+                for (int w = lane; w < TW; w += 32) z = max(z, sm.depth[w]);
+                tileZMax = __reduce_max_sync(0xFFFFFFFFu, z);
+            }
         }
 
         // Pixel (0, 0) centre of the tile in the header frame.
@@ -274,10 +328,6 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
         // MSAA the low word also carries the winner's coverage mask of the
         // pixel (order << 8 | mask) while positions fit in 24 bits.
         const bool packed = S != 0 && count < (1 << 24) - 1;
-        if constexpr (kVisibility) {
-            for (int w = lane; w < TW; w += 32) sm.key[w] = (U64)sm.depth[w] << 32;
-            __syncwarp();
-        }
 
         for (S32 batch = 0; batch < count; batch += 32) {
             if constexpr (kVisibility) {
@@ -312,15 +362,137 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
                                 sm.A[k][lane] = te.A[k];
                                 sm.B[k][lane] = te.B[k];
                             }
-                            sm.td[0][lane] = q0.x;
-                            sm.td[1][lane] = q0.y;
-                            sm.td[2][lane] = q0.z;
+                            sm.z[0][lane] = q0.x;
+                            sm.z[1][lane] = q0.y;
+                            sm.z[2][lane] = q0.z;
                             if (!big) {
                                 n = cnt;
-                                sm.covLo[lane] = (U32)bx0 | (U32)by0 << 4 | (U32)w << 8;
+                                sm.box[lane] = (U32)bx0 | (U32)by0 << 4 | (U32)w << 8;
                                 // Row of box pixel k: (k * ceil(2^16 / w)) >> 16, exact for k < 64, w <= 8.
-                                sm.covHi[lane] = (65536u + (U32)w - 1u) / (U32)w;
+                                sm.mul[lane] = (65536u + (U32)w - 1u) / (U32)w;
                             }
+                        }
+                    }
+                }
+                S32 P = 0;
+                if (__any_sync(0xFFFFFFFFu, n > 0)) {
+                    S32 incl = n;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const S32 t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                        if (lane >= o) incl += t;
+                    }
+                    sm.pairEnd[lane] = incl;
+                    P = __shfl_sync(0xFFFFFFFFu, incl, 31);
+                }
+                __syncwarp();
+                for (S32 base = 0; base < P; base += 32) {
+                    const S32 p = base + lane;
+                    if (p >= P) continue;
+                    int j = 0;
+#pragma unroll
+                    for (int s2 = 16; s2 > 0; s2 >>= 1)
+                        if (sm.pairEnd[j + s2 - 1] <= p) j += s2;
+                    const S32 k = p - (j ? sm.pairEnd[j - 1] : 0);
+                    const U32 bw = sm.box[j];
+                    const S32 w = (S32)(bw >> 8);
+                    const S32 q = (S32)(((U32)k * sm.mul[j]) >> 16);
+                    const S32 px = (S32)(bw & 0xFu) + k - q * w, py = (S32)((bw >> 4) & 0xFu) + q;
+                    const S32 E[3] = {sm.E[0][j], sm.E[1][j], sm.E[2][j]};
+                    const S32 A[3] = {sm.A[0][j], sm.A[1][j], sm.A[2][j]};
+                    const S32 B[3] = {sm.B[0][j], sm.B[1][j], sm.B[2][j]};
+                    const U32 smask = sampleMaskOf<S>(E, A, B, px, py);
+                    if (!smask) continue;
+                    const U32 order = (U32)(batch + j + 1);
+                    const U64 low = packed ? (order << 8 | smask) : order;
+                    const U32 X = (U32)(tx * 8 + px), Y = (U32)(ty * 8 + py);
+                    const U32 zx = sm.z[0][j], zy = sm.z[1][j], zb = sm.z[2][j];
+#pragma unroll
+                    for (int i = 0; i < NS; i++) {
+                        if (!(smask >> i & 1)) continue;
+                        const int idx = py * 8 * NS + i * 8 + px;
+                        const U64 key = ((U64)sampleDepth<S>(zx, zy, zb, X, Y, i) << 32) | low;
+                        if (key < sm.key[idx]) atomicMin((unsigned long long*)&sm.key[idx], (unsigned long long)key);
+                    }
+                }
+                __syncwarp();
+                // Larger triangles: the whole warp, one at a time (each lane
+                // owns its two pixels, so plain stores suffice).
+                const S32 px = lane & 7, py0 = lane >> 3, py1 = py0 + 4;
+                const U32 pX = (U32)(tx * 8 + px), pY0 = (U32)(ty * 8 + py0), pY1 = pY0 + 4;
+                for (U32 m = __ballot_sync(0xFFFFFFFFu, big); m; m &= m - 1) {
+                    const int j = __ffs(m) - 1;
+                    const S32 E[3] = {sm.E[0][j], sm.E[1][j], sm.E[2][j]};
+                    const S32 A[3] = {sm.A[0][j], sm.A[1][j], sm.A[2][j]};
+                    const S32 B[3] = {sm.B[0][j], sm.B[1][j], sm.B[2][j]};
+                    const U32 zx = sm.z[0][j], zy = sm.z[1][j], zb = sm.z[2][j];
+                    const U32 order = (U32)(batch + j + 1);
+#pragma unroll
+                    for (int half = 0; half < 2; half++) {
+                        const S32 pyy = half ? py1 : py0;
+                        const U32 Y = half ? pY1 : pY0;
+                        const U32 smask = sampleMaskOf<S>(E, A, B, px, pyy);
+                        const U64 low = packed ? (order << 8 | smask) : order;
+#pragma unroll
+                        for (int i = 0; i < NS; i++) {
+                            if (!(smask >> i & 1)) continue;
+                            const int idx = pyy * 8 * NS + i * 8 + px;
+                            const U64 key = ((U64)sampleDepth<S>(zx, zy, zb, pX, Y, i) << 32) | low;
+                            if (key < sm.key[idx]) sm.key[idx] = key;
+                        }
+                    }
+                }
+                __syncwarp();
+                // Exact current depth maximum for the next batch's early Z.
+                U32 z = 0;
+                for (int w = lane; w < TW; w += 32) z = max(z, (U32)(sm.key[w] >> 32));
+                tileZMax = __reduce_max_sync(0xFFFFFFFFu, z);
+            } else {
+                // ---- 1. One triangle per lane: its words in shared memory, and
+                // the pixels of the small ones (box of at most selfPixels pixels)
+                // as (triangle, pixel) pairs dealt over the lanes, each setting
+                // the triangle's coverage bit of its pixel (the masks do not
+                // depend on the order the pairs are taken in).
+                bool valid = batch + lane < count;
+                bool self = false;     // small triangle: covered through the pairs
+                U32 myLo = 0, myHi = 0;
+                S32 n = 0;
+                U32* pairBox = sm.pairBox;
+                U32* pairMul = sm.pairMul;
+                sm.covLo[lane] = 0u;
+                sm.covHi[lane] = 0u;
+                if (valid) {
+                    U32 entry = __ldg(&d.tileList[start + batch + lane]);
+                    U32 tri = entry >> 3, sub = entry & 7;
+                    S64 slot = (sub == 7) ? (S64)tri : (S64)__ldg(&d.triHeader[tri].w) + sub;
+                    uint4 h = __ldg(&d.triHeader[slot]);
+                    if (kDepth && (h.w & 0xFFFFF000u) >= tileZMax) valid = false;
+                    if (valid) {
+                        const TileEdges te = tileEdges(h, cx0, cy0);
+                        const uint4* tdp = &d.triData[slot * 4];
+                        uint4 q0 = __ldg(&tdp[0]);
+                        S32 bx0, bx1, by0, by1;
+                        const bool inTile = pixelBox<S>(te, bx0, bx1, by0, by1);
+                        const S32 w = bx1 - bx0 + 1;
+                        self = !inTile || w * (by1 - by0 + 1) <= selfPixels;
+#pragma unroll
+                        for (int k = 0; k < 3; k++) {
+                            sm.E[k][lane] = te.E[k];
+                            sm.A[k][lane] = te.A[k];
+                            sm.B[k][lane] = te.B[k];
+                        }
+                        sm.td[0][lane] = q0.x; sm.td[1][lane] = q0.y; sm.td[2][lane] = q0.z; sm.td[3][lane] = q0.w;
+                        uint4 q1 = __ldg(&tdp[1]), q2 = __ldg(&tdp[2]), q3 = __ldg(&tdp[3]);
+                        sm.td[4][lane] = q1.x; sm.td[5][lane] = q1.y; sm.td[6][lane] = q1.z; sm.td[7][lane] = q1.w;
+                        sm.td[8][lane] = q2.x; sm.td[9][lane] = q2.y; sm.td[10][lane] = q2.z; sm.td[11][lane] = q2.w;
+                        sm.td[12][lane] = q3.x; sm.td[13][lane] = q3.y; sm.td[14][lane] = q3.z; sm.td[15][lane] = q3.w;
+                        sm.tri[lane] = (S32)((S64)tri - triBase);
+                        // No pixel of the tile can be covered (!inTile): nothing to do.
+                        if (inTile && self) {
+                            n = w * (by1 - by0 + 1);
+                            pairBox[lane] = (U32)bx0 | (U32)by0 << 4 | (U32)w << 8;
+                            // Row of box pixel k: (k * ceil(2^16 / w)) >> 16, exact for k < 64, w <= 8.
+                            pairMul[lane] = (65536u + (U32)w - 1u) / (U32)w;
                         }
                     }
                 }
@@ -344,319 +516,197 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
                     for (int s2 = 16; s2 > 0; s2 >>= 1)
                         if (sm.fragEnd[j + s2 - 1] <= p) j += s2;
                     const S32 k = p - (j ? sm.fragEnd[j - 1] : 0);
-                    const U32 bw = sm.covLo[j];
+                    const U32 bw = pairBox[j];
                     const S32 w = (S32)(bw >> 8);
-                    const S32 q = (S32)(((U32)k * sm.covHi[j]) >> 16);
+                    const S32 q = (S32)(((U32)k * pairMul[j]) >> 16);
                     const S32 px = (S32)(bw & 0xFu) + k - q * w, py = (S32)((bw >> 4) & 0xFu) + q;
-                    const S32 E[3] = {sm.E[0][j], sm.E[1][j], sm.E[2][j]};
-                    const S32 A[3] = {sm.A[0][j], sm.A[1][j], sm.A[2][j]};
-                    const S32 B[3] = {sm.B[0][j], sm.B[1][j], sm.B[2][j]};
-                    const U32 smask = sampleMaskOf<S>(E, A, B, px, py);
-                    if (!smask) continue;
-                    const U32 order = (U32)(batch + j + 1);
-                    const U64 low = packed ? (order << 8 | smask) : order;
-                    const U32 X = (U32)(tx * 8 + px), Y = (U32)(ty * 8 + py);
-                    const U32 zx = sm.td[0][j], zy = sm.td[1][j], zb = sm.td[2][j];
+                    const S32 qx = px << kSubpixelLog2, qy = py << kSubpixelLog2;
+                    bool c = true;
 #pragma unroll
-                    for (int i = 0; i < NS; i++) {
-                        if (!(smask >> i & 1)) continue;
-                        const int idx = py * 8 * NS + i * 8 + px;
-                        const U64 key = ((U64)sampleDepth<S>(zx, zy, zb, X, Y, i) << 32) | low;
-                        if (key < sm.key[idx]) atomicMin((unsigned long long*)&sm.key[idx], (unsigned long long)key);
+                    for (int e = 0; e < 3; e++) {
+                        const S32 a = sm.A[e][j], b = sm.B[e][j];
+                        const S32 slack = (S == 0) ? 0 : (abs(a) + abs(b)) << (kSubpixelLog2 - 1);
+                        c = c && (sm.E[e][j] + a * qx + b * qy + slack >= 0);
+                    }
+                    if (kDepth && S == 0 && !kQuads && c) {
+                        const U32 X = (U32)(tx * 8 + px), Y = (U32)(ty * 8 + py);
+                        c = (sm.td[0][j] * X + sm.td[1][j] * Y + sm.td[2][j]) < sm.depth[py * 8 + px];
+                    }
+                    if (c) {
+                        const int bit = py * 8 + px;
+                        atomicOr(bit < 32 ? &sm.covLo[j] : &sm.covHi[j], 1u << (bit & 31));
                     }
                 }
                 __syncwarp();
-                // Larger triangles: the whole warp, one at a time (each lane
-                // owns its two pixels, so plain stores suffice).
+                if (self) {
+                    myLo = sm.covLo[lane];
+                    myHi = sm.covHi[lane];
+                }
+                __syncwarp();
+                const U32 coopMask = __ballot_sync(0xFFFFFFFFu, valid && !self);
+
+                // ---- 2. Large triangles, two pixels per lane.
                 const S32 px = lane & 7, py0 = lane >> 3, py1 = py0 + 4;
                 const U32 pX = (U32)(tx * 8 + px), pY0 = (U32)(ty * 8 + py0), pY1 = pY0 + 4;
-                for (U32 m = __ballot_sync(0xFFFFFFFFu, big); m; m &= m - 1) {
-                    const int j = __ffs(m) - 1;
-                    const S32 E[3] = {sm.E[0][j], sm.E[1][j], sm.E[2][j]};
-                    const S32 A[3] = {sm.A[0][j], sm.A[1][j], sm.A[2][j]};
-                    const S32 B[3] = {sm.B[0][j], sm.B[1][j], sm.B[2][j]};
-                    const U32 zx = sm.td[0][j], zy = sm.td[1][j], zb = sm.td[2][j];
-                    const U32 order = (U32)(batch + j + 1);
+                {
+                    // Single-sample depth of this lane's two pixels at the start of
+                    // the batch: a fragment that fails against it fails in
+                    // submission order too (depths only decrease).
+                    U32 curZ0 = 0, curZ1 = 0;
+                    if (kDepth && S == 0 && !kQuads) {
+                        curZ0 = sm.depth[lane];
+                        curZ1 = sm.depth[lane + 32];
+                    }
+                    const S32 qx = px << kSubpixelLog2, qy0 = py0 << kSubpixelLog2, qy1 = py1 << kSubpixelLog2;
+                    for (U32 m = coopMask; m; m &= m - 1) {
+                        const int j = __ffs(m) - 1;
+                        bool c0 = true, c1 = true;
 #pragma unroll
-                    for (int half = 0; half < 2; half++) {
-                        const S32 pyy = half ? py1 : py0;
-                        const U32 Y = half ? pY1 : pY0;
-                        const U32 smask = sampleMaskOf<S>(E, A, B, px, pyy);
-                        const U64 low = packed ? (order << 8 | smask) : order;
-#pragma unroll
-                        for (int i = 0; i < NS; i++) {
-                            if (!(smask >> i & 1)) continue;
-                            const int idx = pyy * 8 * NS + i * 8 + px;
-                            const U64 key = ((U64)sampleDepth<S>(zx, zy, zb, pX, Y, i) << 32) | low;
-                            if (key < sm.key[idx]) sm.key[idx] = key;
+                        for (int k = 0; k < 3; k++) {
+                            S32 e = sm.E[k][j], a = sm.A[k][j], b = sm.B[k][j];
+                            S32 base = e + a * qx;
+                            S32 slack = (S == 0) ? 0 : (abs(a) + abs(b)) << (kSubpixelLog2 - 1);
+                            c0 = c0 && (base + b * qy0 + slack >= 0);
+                            c1 = c1 && (base + b * qy1 + slack >= 0);
                         }
+                        if (kDepth && S == 0 && !kQuads) {
+                            const U32 zx = sm.td[0][j], zy = sm.td[1][j], zb = sm.td[2][j];
+                            const U32 z0 = zx * pX + zy * pY0 + zb;
+                            c0 = c0 && (z0 < curZ0);
+                            c1 = c1 && (z0 + zy * 4u < curZ1);
+                        }
+                        U32 lo = __ballot_sync(0xFFFFFFFFu, c0);
+                        U32 hi = __ballot_sync(0xFFFFFFFFu, c1);
+                        if (lane == j) { myLo = lo; myHi = hi; }
                     }
                 }
-                __syncwarp();
-                // Exact current depth maximum for the next batch's early Z.
-                U32 z = 0;
-                for (int w = lane; w < TW; w += 32) z = max(z, (U32)(sm.key[w] >> 32));
-                tileZMax = __reduce_max_sync(0xFFFFFFFFu, z);
-                continue;
-            }
-            // ---- 1. One triangle per lane: its words in shared memory, and
-            // the pixels of the small ones (box of at most selfPixels pixels)
-            // as (triangle, pixel) pairs dealt over the lanes, each setting
-            // the triangle's coverage bit of its pixel (the masks do not
-            // depend on the order the pairs are taken in).
-            bool valid = batch + lane < count;
-            bool self = false;     // small triangle: covered through the pairs
-            U32 myLo = 0, myHi = 0;
-            S32 n = 0;
-            U32* pairBox = reinterpret_cast<U32*>(sm.key);        // [32] bx0 | by0 << 4 | w << 8
-            U32* pairMul = reinterpret_cast<U32*>(sm.key) + 32;   // [32] ceil(2^16 / w)
-            sm.covLo[lane] = 0u;
-            sm.covHi[lane] = 0u;
-            if (valid) {
-                U32 entry = __ldg(&d.tileList[start + batch + lane]);
-                U32 tri = entry >> 3, sub = entry & 7;
-                S64 slot = (sub == 7) ? (S64)tri : (S64)__ldg(&d.triHeader[tri].w) + sub;
-                uint4 h = __ldg(&d.triHeader[slot]);
-                if (kDepth && (h.w & 0xFFFFF000u) >= tileZMax) valid = false;
-                if (valid) {
-                    const TileEdges te = tileEdges(h, cx0, cy0);
-                    const uint4* tdp = &d.triData[slot * 4];
-                    uint4 q0 = __ldg(&tdp[0]);
-                    S32 bx0, bx1, by0, by1;
-                    const bool inTile = pixelBox<S>(te, bx0, bx1, by0, by1);
-                    const S32 w = bx1 - bx0 + 1;
-                    self = !inTile || w * (by1 - by0 + 1) <= selfPixels;
-#pragma unroll
-                    for (int k = 0; k < 3; k++) {
-                        sm.E[k][lane] = te.E[k];
-                        sm.A[k][lane] = te.A[k];
-                        sm.B[k][lane] = te.B[k];
-                    }
-                    sm.td[0][lane] = q0.x; sm.td[1][lane] = q0.y; sm.td[2][lane] = q0.z; sm.td[3][lane] = q0.w;
-                    uint4 q1 = __ldg(&tdp[1]), q2 = __ldg(&tdp[2]), q3 = __ldg(&tdp[3]);
-                    sm.td[4][lane] = q1.x; sm.td[5][lane] = q1.y; sm.td[6][lane] = q1.z; sm.td[7][lane] = q1.w;
-                    sm.td[8][lane] = q2.x; sm.td[9][lane] = q2.y; sm.td[10][lane] = q2.z; sm.td[11][lane] = q2.w;
-                    sm.td[12][lane] = q3.x; sm.td[13][lane] = q3.y; sm.td[14][lane] = q3.z; sm.td[15][lane] = q3.w;
-                    sm.tri[lane] = (S32)((S64)tri - triBase);
-                    // No pixel of the tile can be covered (!inTile): nothing to do.
-                    if (inTile && self) {
-                        n = w * (by1 - by0 + 1);
-                        pairBox[lane] = (U32)bx0 | (U32)by0 << 4 | (U32)w << 8;
-                        // Row of box pixel k: (k * ceil(2^16 / w)) >> 16, exact for k < 64, w <= 8.
-                        pairMul[lane] = (65536u + (U32)w - 1u) / (U32)w;
-                    }
+                if (kQuads) {
+                    // quadCoverage (FineRaster.inl:401-406): bit of the quad's top-left pixel.
+                    U64 c = ((U64)myHi << 32) | myLo;
+                    c |= c >> 1;
+                    c |= c >> 8;
+                    c &= 0x0055005500550055ull;
+                    myLo = (U32)c;
+                    myHi = (U32)(c >> 32);
                 }
-            }
-            S32 P = 0;
-            if (__any_sync(0xFFFFFFFFu, n > 0)) {
-                S32 incl = n;
+                if (!valid) { myLo = 0; myHi = 0; }
+
+                // ---- 3. Fragment compaction in submission order.
+                const S32 pop = (__popc(myLo) + __popc(myHi)) * (kQuads ? 4 : 1);
+                S32 inc = pop;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
-                    const S32 t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-                    if (lane >= o) incl += t;
+                    S32 t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+                    if (lane >= o) inc += t;
                 }
-                sm.fragEnd[lane] = incl;
-                P = __shfl_sync(0xFFFFFFFFu, incl, 31);
-            }
-            __syncwarp();
-            for (S32 base = 0; base < P; base += 32) {
-                const S32 p = base + lane;
-                if (p >= P) continue;
-                int j = 0;
-#pragma unroll
-                for (int s2 = 16; s2 > 0; s2 >>= 1)
-                    if (sm.fragEnd[j + s2 - 1] <= p) j += s2;
-                const S32 k = p - (j ? sm.fragEnd[j - 1] : 0);
-                const U32 bw = pairBox[j];
-                const S32 w = (S32)(bw >> 8);
-                const S32 q = (S32)(((U32)k * pairMul[j]) >> 16);
-                const S32 px = (S32)(bw & 0xFu) + k - q * w, py = (S32)((bw >> 4) & 0xFu) + q;
-                const S32 qx = px << kSubpixelLog2, qy = py << kSubpixelLog2;
-                bool c = true;
-#pragma unroll
-                for (int e = 0; e < 3; e++) {
-                    const S32 a = sm.A[e][j], b = sm.B[e][j];
-                    const S32 slack = (S == 0) ? 0 : (abs(a) + abs(b)) << (kSubpixelLog2 - 1);
-                    c = c && (sm.E[e][j] + a * qx + b * qy + slack >= 0);
-                }
-                if (kDepth && S == 0 && !kQuads && c) {
-                    const U32 X = (U32)(tx * 8 + px), Y = (U32)(ty * 8 + py);
-                    c = (sm.td[0][j] * X + sm.td[1][j] * Y + sm.td[2][j]) < sm.depth[py * 8 + px];
-                }
-                if (c) {
-                    const int bit = py * 8 + px;
-                    atomicOr(bit < 32 ? &sm.covLo[j] : &sm.covHi[j], 1u << (bit & 31));
-                }
-            }
-            __syncwarp();
-            if (self) {
-                myLo = sm.covLo[lane];
-                myHi = sm.covHi[lane];
-            }
-            __syncwarp();
-            const U32 coopMask = __ballot_sync(0xFFFFFFFFu, valid && !self);
+                sm.fragEnd[lane] = inc;
+                sm.covLo[lane] = myLo;
+                sm.covHi[lane] = myHi;
+                const S32 total = __shfl_sync(0xFFFFFFFFu, inc, 31);
+                __syncwarp();
 
-            // ---- 2. Large triangles, two pixels per lane.
-            const S32 px = lane & 7, py0 = lane >> 3, py1 = py0 + 4;
-            const U32 pX = (U32)(tx * 8 + px), pY0 = (U32)(ty * 8 + py0), pY1 = pY0 + 4;
-            {
-                // Single-sample depth of this lane's two pixels at the start of
-                // the batch: a fragment that fails against it fails in
-                // submission order too (depths only decrease).
-                U32 curZ0 = 0, curZ1 = 0;
-                if (kDepth && S == 0 && !kQuads) {
-                    curZ0 = sm.depth[lane];
-                    curZ1 = sm.depth[lane + 32];
-                }
-                const S32 qx = px << kSubpixelLog2, qy0 = py0 << kSubpixelLog2, qy1 = py1 << kSubpixelLog2;
-                for (U32 m = coopMask; m; m &= m - 1) {
-                    const int j = __ffs(m) - 1;
-                    bool c0 = true, c1 = true;
-#pragma unroll
-                    for (int k = 0; k < 3; k++) {
-                        S32 e = sm.E[k][j], a = sm.A[k][j], b = sm.B[k][j];
-                        S32 base = e + a * qx;
-                        S32 slack = (S == 0) ? 0 : (abs(a) + abs(b)) << (kSubpixelLog2 - 1);
-                        c0 = c0 && (base + b * qy0 + slack >= 0);
-                        c1 = c1 && (base + b * qy1 + slack >= 0);
-                    }
-                    if (kDepth && S == 0 && !kQuads) {
-                        const U32 zx = sm.td[0][j], zy = sm.td[1][j], zb = sm.td[2][j];
-                        const U32 z0 = zx * pX + zy * pY0 + zb;
-                        c0 = c0 && (z0 < curZ0);
-                        c1 = c1 && (z0 + zy * 4u < curZ1);
-                    }
-                    U32 lo = __ballot_sync(0xFFFFFFFFu, c0);
-                    U32 hi = __ballot_sync(0xFFFFFFFFu, c1);
-                    if (lane == j) { myLo = lo; myHi = hi; }
-                }
-            }
-            if (kQuads) {
-                // quadCoverage (FineRaster.inl:401-406): bit of the quad's top-left pixel.
-                U64 c = ((U64)myHi << 32) | myLo;
-                c |= c >> 1;
-                c |= c >> 8;
-                c &= 0x0055005500550055ull;
-                myLo = (U32)c;
-                myHi = (U32)(c >> 32);
-            }
-            if (!valid) { myLo = 0; myHi = 0; }
-
-            // ---- 3. Fragment compaction in submission order.
-            const S32 pop = (__popc(myLo) + __popc(myHi)) * (kQuads ? 4 : 1);
-            S32 inc = pop;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                S32 t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
-                if (lane >= o) inc += t;
-            }
-            sm.fragEnd[lane] = inc;
-            sm.covLo[lane] = myLo;
-            sm.covHi[lane] = myHi;
-            const S32 total = __shfl_sync(0xFFFFFFFFu, inc, 31);
-            __syncwarp();
-
-            for (S32 pass = 0; pass < total; pass += 32) {
-                const S32 f = pass + lane;
-                bool act = f < total;
-                int j = 0, pixel = 0;
-                bool covered = false;
-                U32 sampleMask = 0;
-                U32 dz[NS];
-                if (act) {
-                    // Triangle of fragment f: first j with fragEnd[j] > f.
-                    int lo = 0, hi = 31;
-                    while (lo < hi) {
-                        int mid = (lo + hi) >> 1;
-                        if (sm.fragEnd[mid] > f) hi = mid; else lo = mid + 1;
-                    }
-                    j = lo;
-                    const U32 cl = sm.covLo[j], ch = sm.covHi[j];
-                    const S32 k = f - (sm.fragEnd[j] - (S32)((__popc(cl) + __popc(ch)) * (kQuads ? 4 : 1)));
-                    if (kQuads) {
-                        int qbit = nthSetBit64(cl, ch, k >> 2);
-                        pixel = qbit + (k & 1) + ((k & 2) << 2);  // findFragment, FineRaster.inl:417-427
-                    } else {
-                        pixel = nthSetBit64(cl, ch, k);
-                    }
-                    const S32 fx = pixel & 7, fy = pixel >> 3;
-                    if (S == 0 && !kQuads) {
-                        sampleMask = 1;  // single-sample masks are exact
-                    } else {
-                        const S32 E[3] = {sm.E[0][j], sm.E[1][j], sm.E[2][j]};
-                        const S32 A[3] = {sm.A[0][j], sm.A[1][j], sm.A[2][j]};
-                        const S32 B[3] = {sm.B[0][j], sm.B[1][j], sm.B[2][j]};
-                        sampleMask = sampleMaskOf<S>(E, A, B, fx, fy);
-                    }
-                    covered = sampleMask != 0;
-                    if (!kQuads && !covered) act = false;
-                    const U32 X = (U32)(tx * 8 + fx), Y = (U32)(ty * 8 + fy);
-                    if (kDepth) {
-                        const U32 zx = sm.td[0][j], zy = sm.td[1][j], zb = sm.td[2][j];
-                        bool anyPass = false;
-                        const int rowBase = fy * 8 * NS + fx;
-#pragma unroll
-                        for (int i = 0; i < NS; i++) {
-                            dz[i] = sampleDepth<S>(zx, zy, zb, X, Y, i);
-                            if ((sampleMask >> i & 1) && dz[i] < sm.depth[rowBase + i * 8]) anyPass = true;
+                for (S32 pass = 0; pass < total; pass += 32) {
+                    const S32 f = pass + lane;
+                    bool act = f < total;
+                    int j = 0, pixel = 0;
+                    bool covered = false;
+                    U32 sampleMask = 0;
+                    U32 dz[NS];
+                    if (act) {
+                        // Triangle of fragment f: first j with fragEnd[j] > f.
+                        int lo = 0, hi = 31;
+                        while (lo < hi) {
+                            int mid = (lo + hi) >> 1;
+                            if (sm.fragEnd[mid] > f) hi = mid; else lo = mid + 1;
                         }
-                        if (!kQuads && !anyPass) act = false;
-                        if (kQuads && !anyPass) covered = false;
-                    }
-                }
-                // Shade.
-                const U32 shadeMask = __ballot_sync(0xFFFFFFFFu, act);
-                U32 src = 0;
-                bool discard = true;
-                if (act) {
-                    U32 td[16];
-#pragma unroll
-                    for (int q = 0; q < 16; q++) td[q] = sm.td[q][j];
-                    src = shadeFragment<FS, S, F>(td, sm.tri[j], tx * 8 + (pixel & 7), ty * 8 + (pixel >> 3), sampleMask,
-                                                  verts, stride4, sm.shared, shadeMask, discard);
-                }
-                // ROP: same-pixel fragments of this pass applied in lane order.
-                const bool rop = act && covered && !discard;
-                const U32 ropMask = __ballot_sync(0xFFFFFFFFu, rop);
-                if (ropMask) {
-                    U32 peers = 0;
-                    if (rop) peers = __match_any_sync(ropMask, pixel);
-                    const int rank = __popc(peers & ltMask);
-                    const int maxGroup = __reduce_max_sync(0xFFFFFFFFu, rop ? __popc(peers) : 0);
-                    for (int r = 0; r < maxGroup; r++) {
-                        if (rop && rank == r) {
-                            const S32 fx = pixel & 7, fy = pixel >> 3;
+                        j = lo;
+                        const U32 cl = sm.covLo[j], ch = sm.covHi[j];
+                        const S32 k = f - (sm.fragEnd[j] - (S32)((__popc(cl) + __popc(ch)) * (kQuads ? 4 : 1)));
+                        if (kQuads) {
+                            int qbit = nthSetBit64(cl, ch, k >> 2);
+                            pixel = qbit + (k & 1) + ((k & 2) << 2);  // findFragment, FineRaster.inl:417-427
+                        } else {
+                            pixel = nthSetBit64(cl, ch, k);
+                        }
+                        const S32 fx = pixel & 7, fy = pixel >> 3;
+                        if (S == 0 && !kQuads) {
+                            sampleMask = 1;  // single-sample masks are exact
+                        } else {
+                            const S32 E[3] = {sm.E[0][j], sm.E[1][j], sm.E[2][j]};
+                            const S32 A[3] = {sm.A[0][j], sm.A[1][j], sm.A[2][j]};
+                            const S32 B[3] = {sm.B[0][j], sm.B[1][j], sm.B[2][j]};
+                            sampleMask = sampleMaskOf<S>(E, A, B, fx, fy);
+                        }
+                        covered = sampleMask != 0;
+                        if (!kQuads && !covered) act = false;
+                        const U32 X = (U32)(tx * 8 + fx), Y = (U32)(ty * 8 + fy);
+                        if (kDepth) {
+                            const U32 zx = sm.td[0][j], zy = sm.td[1][j], zb = sm.td[2][j];
+                            bool anyPass = false;
                             const int rowBase = fy * 8 * NS + fx;
-                            BS bs;
 #pragma unroll
                             for (int i = 0; i < NS; i++) {
-                                if (!(sampleMask >> i & 1)) continue;
-                                const int idx = rowBase + i * 8;
-                                if (kDepth) {
-                                    if (!(dz[i] < sm.depth[idx])) continue;
-                                    sm.depth[idx] = dz[i];
-                                }
-                                bs.m_triIdx = sm.tri[j];
-                                bs.m_pixelPos = FW::Vec2i(tx * 8 + fx, ty * 8 + fy);
-                                bs.m_sampleIdx = i;
-                                bs.m_src = src;
-                                bs.m_dst = sm.color[idx];
-                                bs.m_color = 0xFF0000FFu;
-                                bs.m_writeColor = true;
-                                bs.run();
-                                if (bs.m_writeColor) sm.color[idx] = bs.m_color;
+                                dz[i] = sampleDepth<S>(zx, zy, zb, X, Y, i);
+                                if ((sampleMask >> i & 1) && dz[i] < sm.depth[rowBase + i * 8]) anyPass = true;
                             }
+                            if (!kQuads && !anyPass) act = false;
+                            if (kQuads && !anyPass) covered = false;
                         }
-                        __syncwarp();
+                    }
+                    // Shade.
+                    const U32 shadeMask = __ballot_sync(0xFFFFFFFFu, act);
+                    U32 src = 0;
+                    bool discard = true;
+                    if (act) {
+                        U32 td[16];
+#pragma unroll
+                        for (int q = 0; q < 16; q++) td[q] = sm.td[q][j];
+                        src = shadeFragment<FS, S, F>(td, sm.tri[j], tx * 8 + (pixel & 7), ty * 8 + (pixel >> 3), sampleMask,
+                                                      verts, stride4, sm.shared, shadeMask, discard);
+                    }
+                    // ROP: same-pixel fragments of this pass applied in lane order.
+                    const bool rop = act && covered && !discard;
+                    const U32 ropMask = __ballot_sync(0xFFFFFFFFu, rop);
+                    if (ropMask) {
+                        U32 peers = 0;
+                        if (rop) peers = __match_any_sync(ropMask, pixel);
+                        const int rank = __popc(peers & ltMask);
+                        const int maxGroup = __reduce_max_sync(0xFFFFFFFFu, rop ? __popc(peers) : 0);
+                        for (int r = 0; r < maxGroup; r++) {
+                            if (rop && rank == r) {
+                                const S32 fx = pixel & 7, fy = pixel >> 3;
+                                const int rowBase = fy * 8 * NS + fx;
+                                BS bs;
+#pragma unroll
+                                for (int i = 0; i < NS; i++) {
+                                    if (!(sampleMask >> i & 1)) continue;
+                                    const int idx = rowBase + i * 8;
+                                    if (kDepth) {
+                                        if (!(dz[i] < sm.depth[idx])) continue;
+                                        sm.depth[idx] = dz[i];
+                                    }
+                                    bs.m_triIdx = sm.tri[j];
+                                    bs.m_pixelPos = FW::Vec2i(tx * 8 + fx, ty * 8 + fy);
+                                    bs.m_sampleIdx = i;
+                                    bs.m_src = src;
+                                    bs.m_dst = sm.color[idx];
+                                    bs.m_color = 0xFF0000FFu;
+                                    bs.m_writeColor = true;
+                                    bs.run();
+                                    if (bs.m_writeColor) sm.color[idx] = bs.m_color;
+                                }
+                            }
+                            __syncwarp();
+                        }
                     }
                 }
+                if (kDepth) {
+                    U32 z = 0;
+                    for (int w = lane; w < TW; w += 32) z = max(z, sm.depth[w]);
+                    tileZMax = __reduce_max_sync(0xFFFFFFFFu, z);
+                }
+                __syncwarp();
             }
-            if (kDepth) {
-                U32 z = 0;
-                for (int w = lane; w < TW; w += 32) z = max(z, sm.depth[w]);
-                tileZMax = __reduce_max_sync(0xFFFFFFFFu, z);
-            }
-            __syncwarp();
         }
 
         if constexpr (kVisibility) {
@@ -668,9 +718,7 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
             // lane owns pixels lane and lane + 32), then fetched and shaded
             // 32 at a time, so lanes stay busy however unevenly the winners
             // fall on the pixels and samples.
-            // Winner records (pixel | first sample << 6 | samples won << 9), at
-            // most 64 << S <= 512 of them, in the triangle words (free by now).
-            U32* winners = &sm.td[0][0];
+            U32* winners = sm.winners;
             S32 nw = 0;
 #pragma unroll
             for (int hh = 0; hh < 2; hh++) {
@@ -743,7 +791,6 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
                 for (int i = 0; i < NS; i++) {
                     if (!(won >> i & 1)) continue;
                     const int idx = rowBase + i * 8;
-                    sm.depth[idx] = (U32)(sm.key[idx] >> 32);
                     bs.m_triIdx = triIdx;
                     bs.m_pixelPos = FW::Vec2i(X, Y);
                     bs.m_sampleIdx = i;
@@ -762,10 +809,33 @@ __global__ void __launch_bounds__(kFineMaxThreads) fineKernel(DrawDev d, int gro
         for (int w = lane; w < TW; w += 32) {
             S64 g = tileOrigin + (S64)(w / (8 * NS)) * rowWords + (w % (8 * NS));
             gColor[g] = sm.color[w];
-            gDepth[g] = sm.depth[w];
+            if constexpr (kVisibility)
+                gDepth[g] = (U32)(sm.key[w] >> 32);
+            else
+                gDepth[g] = sm.depth[w];
         }
         __syncwarp();
     }
+}
+
+// The fine-stage kernel. At one sample the register budget is pinned to five
+// resident CTAs per SM (48 registers); with MSAA the compiler's own choice
+// measured faster than any pinned budget (4x MSAA: 63 registers, 0.58 ms on
+// the 4K grid, against 0.60 ms pinned to four CTAs and 0.64 ms to three).
+template <class V, class FS, class BS, int S, U32 F>
+__global__ void __launch_bounds__(kFineMaxThreads, 5) fineKernel1(DrawDev d, int group, S32 tileBegin, S32 tileEnd) {
+    fineTiles<V, FS, BS, S, F>(d, group, tileBegin, tileEnd);
+}
+template <class V, class FS, class BS, int S, U32 F>
+__global__ void __launch_bounds__(kFineMaxThreads) fineKernelMsaa(DrawDev d, int group, S32 tileBegin, S32 tileEnd) {
+    fineTiles<V, FS, BS, S, F>(d, group, tileBegin, tileEnd);
+}
+template <class V, class FS, class BS, int S, U32 F>
+constexpr auto fineKernelFor() {
+    if constexpr (S == 0)
+        return &fineKernel1<V, FS, BS, S, F>;
+    else
+        return &fineKernelMsaa<V, FS, BS, S, F>;
 }
 
 }  // namespace cr
