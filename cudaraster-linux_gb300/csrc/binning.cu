@@ -71,22 +71,32 @@ struct GroupSmem {
 
 // Publishes a group of up to 32 list items (lane i: item entry, if valid)
 // with their cell boxes; returns the group's number of (item, cell) pairs
-// and the lane's inclusive prefix of them in incl.
+// and the lane's inclusive prefix of them in incl -- or -1 when no item has
+// more than one cell, with the lane's own cell (or -1) in cell1.
 __device__ __forceinline__ S32 stageItems(const DrawDev& d, const Grid& gr, bool valid, U32 entry, GroupSmem& gs,
-                                          S32& incl) {
+                                          S32& incl, int& cell1) {
     const int lane = threadIdx.x & 31;
     S32 n = 0;
-    U32 box = 0, mul = 0;
+    CellBox b{};
     uint4 h = make_uint4(0u, 0u, 0u, 0u);
     if (valid) {
         h = __ldg(&d.triHeader[entrySlot(entry, d.triHeader)]);
-        const CellBox b = cellBox(geomFromHeader(h), gr.halfW, gr.halfH, gr.cellLog2, gr.cx0, gr.cy0, gr.cx1, gr.cy1);
+        b = cellBox(geomFromHeader(h), gr.halfW, gr.halfH, gr.cellLog2, gr.cx0, gr.cy0, gr.cx1, gr.cy1);
         n = b.count();
-        if (n > 0) {
-            const U32 w = (U32)(b.hx - b.lx + 1);
-            box = (U32)(b.lx - gr.cx0) | (U32)(b.ly - gr.cy0) << 8 | w << 16 | (b.small() ? 1u << 31 : 0u);
-            mul = ((1u << 20) + w - 1u) / w;
-        }
+    }
+    gs.entry[lane] = entry;
+    // Every item in at most one cell (the common case for small triangles):
+    // the pairs are the items themselves, no expansion needed.
+    if (__all_sync(0xFFFFFFFFu, n <= 1)) {
+        cell1 = n == 1 ? (b.ly - gr.cy0) * gr.stride + (b.lx - gr.cx0) : -1;
+        __syncwarp();
+        return -1;
+    }
+    U32 box = 0, mul = 0;
+    if (n > 0) {
+        const U32 w = (U32)(b.hx - b.lx + 1);
+        box = (U32)(b.lx - gr.cx0) | (U32)(b.ly - gr.cy0) << 8 | w << 16 | (b.small() ? 1u << 31 : 0u);
+        mul = ((1u << 20) + w - 1u) / w;
     }
     incl = warpInclusiveScan(n);
     gs.incl[lane] = incl;
@@ -95,7 +105,6 @@ __device__ __forceinline__ S32 stageItems(const DrawDev& d, const Grid& gr, bool
     gs.v[2][lane] = h.z;
     gs.box[lane] = box;
     gs.mul[lane] = mul;
-    gs.entry[lane] = entry;
     __syncwarp();
     return __shfl_sync(0xFFFFFFFFu, incl, 31);
 }
@@ -207,7 +216,12 @@ __device__ __forceinline__ void walkSlice(const DrawDev& d, const Grid& gr, S64 
         head = (head + g) & (kRing - 1);
         fill -= g;
         S32 incl;
-        const S32 P = stageItems(d, gr, valid, entry, gs, incl);
+        int cell1;
+        const S32 P = stageItems(d, gr, valid, entry, gs, incl, cell1);
+        if (P < 0) {
+            const bool hit = cell1 >= 0;
+            fn(hit, cell1, lane, __match_any_sync(0xFFFFFFFFu, hit ? (U32)cell1 : 0x10000u + (U32)lane));
+        }
         for (S32 base = 0; base < P; base += 32) {
             const S32 p = base + lane;
             int j = 0, cell = 0;
@@ -455,8 +469,10 @@ __global__ void __launch_bounds__(kCoarseThreads) coarseCountKernel(DrawDev d) {
         __syncwarp();
         for (S32 e0 = ui.e0; e0 < ui.e1; e0 += 32) {
             S32 incl;
+            int cell1;
             const bool valid = e0 + lane < ui.e1;
-            const S32 P = stageItems(d, gr, valid, valid ? __ldg(&d.binList[e0 + lane]) : 0u, gs, incl);
+            const S32 P = stageItems(d, gr, valid, valid ? __ldg(&d.binList[e0 + lane]) : 0u, gs, incl, cell1);
+            if (P < 0 && cell1 >= 0) atomicAdd(&cnt[cell1], 1);
             for (S32 p = lane; p < P; p += 32) {
                 int j, cell;
                 if (pairCell(gs, gr, p, j, cell)) atomicAdd(&cnt[cell], 1);
@@ -582,8 +598,20 @@ __global__ void __launch_bounds__(kCoarseThreads) coarseScatterKernel(DrawDev d)
         __syncwarp();
         for (S32 e0 = ui.e0; e0 < ui.e1; e0 += 32) {
             S32 incl;
+            int cell1;
             const bool valid = e0 + lane < ui.e1;
-            const S32 P = stageItems(d, gr, valid, valid ? __ldg(&d.binList[e0 + lane]) : 0u, gs, incl);
+            const S32 P = stageItems(d, gr, valid, valid ? __ldg(&d.binList[e0 + lane]) : 0u, gs, incl, cell1);
+            if (P < 0) {
+                const bool hit = cell1 >= 0;
+                const U32 peers = __match_any_sync(0xFFFFFFFFu, hit ? (U32)cell1 : 0x10000u + (U32)lane);
+                if (hit) {
+                    const S64 idx = (S64)run[cell1] + __popc(peers & ltMask);
+                    if (idx < d.maxTileEntries) d.tileList[idx] = gs.entry[lane];
+                }
+                __syncwarp();
+                if (hit && (peers >> lane) == 1u) run[cell1] += __popc(peers);
+                __syncwarp();
+            }
             for (S32 base = 0; base < P; base += 32) {
                 const S32 p = base + lane;
                 int j = 0, cell = 0;
