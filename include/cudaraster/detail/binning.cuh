@@ -39,33 +39,6 @@ __device__ __forceinline__ bool triTouchesRect(const TriGeom& g, S32 rx0, S32 ry
            edgeTouchesRect(g.x2, g.y2, g.x0 - g.x2, g.y0 - g.y2, rx0, ry0, rx1, ry1);
 }
 
-// Cells of side 2^cellLog2 subpixels over a grid of gw x gh cells whose
-// origin is the viewport's top-left corner (header frame offset by half the
-// viewport). Calls fn(cx, cy) for every cell the triangle may touch, in
-// row-major order, restricted to [cx0, cx1] x [cy0, cy1].
-template <class Fn>
-__device__ __forceinline__ void forEachCell(const TriGeom& g, S32 halfW, S32 halfH, int cellLog2,
-                                            S32 cx0, S32 cy0, S32 cx1, S32 cy1, Fn fn) {
-    S32 lx = (min3i(g.x0, g.x1, g.x2) + halfW) >> cellLog2;
-    S32 hx = (max3i(g.x0, g.x1, g.x2) + halfW) >> cellLog2;
-    S32 ly = (min3i(g.y0, g.y1, g.y2) + halfH) >> cellLog2;
-    S32 hy = (max3i(g.y0, g.y1, g.y2) + halfH) >> cellLog2;
-    lx = max(lx, cx0); ly = max(ly, cy0);
-    hx = min(hx, cx1); hy = min(hy, cy1);
-    if (lx > hx || ly > hy) return;
-    const bool small = (hx - lx) <= 1 && (hy - ly) <= 1;
-    const S32 cell = 1 << cellLog2;
-    for (S32 cy = ly; cy <= hy; cy++) {
-        for (S32 cx = lx; cx <= hx; cx++) {
-            if (!small) {
-                S32 rx0 = (cx << cellLog2) - halfW, ry0 = (cy << cellLog2) - halfH;
-                if (!triTouchesRect(g, rx0, ry0, rx0 + cell - 1, ry0 + cell - 1)) continue;
-            }
-            fn(cx, cy);
-        }
-    }
-}
-
 // Cell range of a triangle's bounding box, clamped to [cx0, cx1] x [cy0, cy1].
 struct CellBox {
     S32 lx, ly, hx, hy;
@@ -81,16 +54,6 @@ __device__ __forceinline__ CellBox cellBox(const TriGeom& g, S32 halfW, S32 half
     b.ly = max((min3i(g.y0, g.y1, g.y2) + halfH) >> cellLog2, cy0);
     b.hy = min((max3i(g.y0, g.y1, g.y2) + halfH) >> cellLog2, cy1);
     return b;
-}
-
-// Is cell (cx, cy) of box b touched by the triangle? (bbox shortcut for boxes
-// of at most 2x2 cells, as the reference's bin/coarse fast paths.)
-__device__ __forceinline__ bool cellTouched(const TriGeom& g, const CellBox& b, S32 cx, S32 cy, S32 halfW, S32 halfH,
-                                            int cellLog2) {
-    if (b.small()) return true;
-    const S32 cell = 1 << cellLog2;
-    S32 rx0 = (cx << cellLog2) - halfW, ry0 = (cy << cellLog2) - halfH;
-    return triTouchesRect(g, rx0, ry0, rx0 + cell - 1, ry0 + cell - 1);
 }
 
 // List entry <-> data slot: entry = triangle << 3 | subtriangle, 7 = the
