@@ -460,7 +460,7 @@ __global__ void __launch_bounds__(kCoarseThreads) coarseCountKernel(DrawDev d) {
     const S32 numUnits = (S32)min((S64)__ldg(&d.counters->numUnits), d.maxUnits);
     const S32 unitEntries = __ldg(&d.counters->unitEntries);
     for (;;) {
-        const int u = warpNextUnit(&d.counters->coarseWork[0]);
+        const int u = warpNextUnit(&d.counters->coarseWork[0]);   // count pass
         if (u >= numUnits) break;
         UnitInfo ui;
         loadUnit(d, u, unitEntries, ui);

@@ -7,9 +7,13 @@
 // the tile's current maximum depth as FineRaster.inl:229-240, edge functions
 // at the tile origin). Then one of two algorithms runs, chosen at compile time:
 //
+// Both paths deal the (triangle, pixel) pairs of the batch's small triangles
+// (pixel box of at most fineSelfPixels pixels) over the lanes; larger
+// triangles are rasterized by the 32 pixel-owning lanes, two pixels each.
+//
 // Ordered path (any blend shader, discard, quads):
-//   coverage masks per triangle (small triangles by their own lane, large ones
-//   by the 32 pixel-owning lanes with ballots), covered pixels compacted into
+//   coverage masks per triangle (set by the pairs, or by ballots over the
+//   pixel-owning lanes for large triangles), covered pixels compacted into
 //   passes of 32 fragments in submission order (FineRaster.inl:625-731), then
 //   depth test, shading and blending per fragment. Fragments of one pass that
 //   hit the same pixel are grouped with __match_any_sync and applied one rank
@@ -23,7 +27,8 @@
 //   submission order on equal depth -- the same result as applying every
 //   fragment in order with a LESS test. Each sample keeps a 64-bit key
 //   (depth << 32 | list position + 1) that fragments lower with atomicMin;
-//   after the list, every sample's winner is shaded once.
+//   after the list, the tile's winners are listed and each is shaded once,
+//   32 at a time.
 //
 // MSAA keeps every sample of the tile in shared memory (reference layout:
 // sample i of pixel x at word i * 8 + x of the tile row) and shades once per
