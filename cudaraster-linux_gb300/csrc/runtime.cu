@@ -959,7 +959,7 @@ cr_status cr_get_profiling_info(cr_context* ctx, char* buffer, int64_t size) {
     cr_stats s;
     cr_status st = cr_get_stats(ctx, &s);
     if (st != CR_OK) return st;
-    cr_counters c;
+    cr_counters c{};
     cr_get_counters(ctx, &c);
     // Format follows getProfilingInfo's default mode (CudaRaster.cpp:367-421):
     // stage times, then the memory footprint of the intermediate queues.

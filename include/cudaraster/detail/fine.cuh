@@ -552,7 +552,7 @@ __device__ __forceinline__ void fineTiles(const DrawDev& d, int group, S32 tileB
 
                 // ---- 2. Large triangles, two pixels per lane.
                 const S32 px = lane & 7, py0 = lane >> 3, py1 = py0 + 4;
-                const U32 pX = (U32)(tx * 8 + px), pY0 = (U32)(ty * 8 + py0), pY1 = pY0 + 4;
+                const U32 pX = (U32)(tx * 8 + px), pY0 = (U32)(ty * 8 + py0);
                 {
                     // Single-sample depth of this lane's two pixels at the start of
                     // the batch: a fragment that fails against it fails in
