@@ -251,9 +251,10 @@ def main():
     ap.add_argument("--profile-frames", type=int, default=0,
                     help="only draw this many frames of the workload (for ncu captures), print nothing else")
     ap.add_argument("--profile-workload", default="soup1m", choices=["soup1m", "subpixel", "flythrough", "flythrough2048",
-                                                              "predicted"],
+                                                              "predicted", "batch64"],
                     help="workload of --profile-frames: the 1M soup (default), the 4x MSAA heightfield, plain "
-                         "fly-through frames, or predictor-sized fly-through frames (12 of them, 8 training)")
+                         "fly-through frames, predictor-sized fly-through frames (12 of them, 8 training) or "
+                         "replays of the uneven 64-scene batch")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))

@@ -496,8 +496,24 @@ def profile_frames(name: str, frames: int, tuning: dict | None = None) -> dict:
     """Draws a few frames of a workload and nothing else (for profiler runs):
     "subpixel" (the 4x MSAA heightfield), "flythrough" / "flythrough2048"
     (plain fly-through frames 100..100+frames over the 4096^2 or a 2048^2
-    heightfield) or "predicted" (a short predictor-sized
-    fly-through: `frames` frames, the first two thirds plain and training)."""
+    heightfield), "predicted" (a short predictor-sized fly-through: `frames`
+    frames, the first two thirds plain and training) or "batch64" (`frames`
+    replays of the uneven 64-scene batch's CUDA graph)."""
+    if name == "batch64":
+        p = _pkg()
+        scenes = importlib.import_module(PKG + ".scenes")
+        batch = Batch(scenes.batch(64, seed=4))
+        cr = p.CudaRaster()
+        cr.init()
+        if tuning:
+            cr.setTuning(**tuning)
+        g = cr.createBatchGraph(batch.items)
+        stream = torch.cuda.current_stream()
+        for _ in range(frames):
+            g.launch(stream)
+        torch.cuda.synchronize()
+        g.destroy()
+        return {"profile": name, "frames": frames, "tris": batch.num_tris}
     if name == "subpixel":
         s, _, _ = measure_subpixel(steps=frames, warmup=0, tuning=tuning)
         return {"profile": name, "frames": frames, "counters": s["counters"]}
