@@ -59,6 +59,10 @@ class Instance(C.Structure):
                 ("clear_color", C.c_uint32), ("clear_depth", C.c_uint32)]
 
 
+class VertexConstants(C.Structure):
+    _fields_ = [("pos_to_clip", C.c_float * 16), ("pos_to_camera", C.c_float * 16), ("normal_to_camera", C.c_float * 9)]
+
+
 class QueueLayout(C.Structure):
     _fields_ = [("bins_x", C.c_int32), ("bins_y", C.c_int32), ("tiles_x", C.c_int32), ("tiles_y", C.c_int32),
                 ("bin_log2", C.c_int32), ("num_bins", C.c_int32), ("num_tiles", C.c_int32),
@@ -95,6 +99,11 @@ _SIGNATURES = {
                                            C.c_void_p, C.c_char_p, C.c_int64]),
     "cr_vertex_shader_passthrough": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
                                                C.c_int64, C.POINTER(C.c_float), C.c_void_p]),
+    "cr_vertex_shader_gouraud": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(VertexConstants), C.c_void_p, C.c_int32,
+                                           C.c_void_p, C.c_void_p, C.c_void_p]),
+    "cr_vertex_shader_tex_phong": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(VertexConstants), C.c_void_p,
+                                             C.c_void_p]),
+    "cr_pow_exact": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     "cr_resolve_color": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p]),
     "cr_get_queue_layout": (C.c_int, [C.c_void_p, C.POINTER(QueueLayout)]),
     "cr_queue_counts": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),

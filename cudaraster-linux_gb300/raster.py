@@ -372,6 +372,57 @@ def vertex_shader_passthrough(model: torch.Tensor, mvp, colors: torch.Tensor | N
     return out
 
 
+def _vertex_constants(pos_to_clip, pos_to_camera, normal_to_camera):
+    k = _lib.VertexConstants()
+    for name, m, n in (("pos_to_clip", pos_to_clip, 16), ("pos_to_camera", pos_to_camera, 16),
+                       ("normal_to_camera", normal_to_camera, 9)):
+        vals = [float(x) for x in torch.as_tensor(m, dtype=torch.float32).reshape(-1).tolist()]
+        if len(vals) != n:
+            raise RasterError(1, f"{name} needs {n} values")
+        getattr(k, name)[:] = vals
+    return k
+
+
+def vertex_shader_gouraud(vertices: torch.Tensor, pos_to_clip, pos_to_camera, normal_to_camera,
+                          materials: torch.Tensor, material_idx: torch.Tensor, out: torch.Tensor | None = None,
+                          stream: torch.cuda.Stream | None = None) -> torch.Tensor:
+    """The reference's vertexShader_gouraud on the GPU. vertices: [N, 8] InputVertex
+    records (position, normal, texture coordinate); materials: [M, 8] (diffuse rgba,
+    specular rgb, glossiness); material_idx: [N] int32. Returns [N, 8] GouraudVertex
+    records (clip position, lit colour)."""
+    lib = _lib.load()
+    n = vertices.shape[0]
+    if out is None:
+        out = torch.empty((n, 8), dtype=torch.float32, device=vertices.device)
+    k = _vertex_constants(pos_to_clip, pos_to_camera, normal_to_camera)
+    s = (stream or torch.cuda.current_stream()).cuda_stream
+    check(lib.cr_vertex_shader_gouraud(vertices.data_ptr(), n, C.byref(k), materials.data_ptr(), materials.shape[0],
+                                       material_idx.data_ptr(), out.data_ptr(), C.c_void_p(s)))
+    return out
+
+
+def vertex_shader_tex_phong(vertices: torch.Tensor, pos_to_clip, pos_to_camera, normal_to_camera,
+                            out: torch.Tensor | None = None, stream: torch.cuda.Stream | None = None) -> torch.Tensor:
+    """The reference's vertexShader_texPhong on the GPU: [N, 8] InputVertex records ->
+    [N, 16] ShadedVertex_texPhong records."""
+    lib = _lib.load()
+    n = vertices.shape[0]
+    if out is None:
+        out = torch.empty((n, 16), dtype=torch.float32, device=vertices.device)
+    k = _vertex_constants(pos_to_clip, pos_to_camera, normal_to_camera)
+    s = (stream or torch.cuda.current_stream()).cuda_stream
+    check(lib.cr_vertex_shader_tex_phong(vertices.data_ptr(), n, C.byref(k), out.data_ptr(), C.c_void_p(s)))
+    return out
+
+
+def pow_exact(x: torch.Tensor, y: torch.Tensor, stream: torch.cuda.Stream | None = None) -> torch.Tensor:
+    """The vertex lighting's exact power, elementwise on float32 CUDA tensors."""
+    out = torch.empty_like(x)
+    s = (stream or torch.cuda.current_stream()).cuda_stream
+    check(_lib.load().cr_pow_exact(x.data_ptr(), y.data_ptr(), out.data_ptr(), x.numel(), C.c_void_p(s)))
+    return out
+
+
 def vertex_shader_reference(model, mvp):
     """Host restatement (numpy float32) of the same product, used by tests."""
     import numpy as np

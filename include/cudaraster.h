@@ -221,6 +221,39 @@ cr_status cr_vertex_shader_passthrough(const float* model, int32_t model_stride,
                                        int32_t color_stride, void* out_vertices, int32_t out_stride_bytes,
                                        int64_t num_vertices, const float* mvp_row_major, void* stream);
 
+/* The reference's Constants (test/shader/Shaders.hpp) for its vertex shaders:
+ * row-major matrices. */
+typedef struct cr_vertex_constants {
+    float pos_to_clip[16];
+    float pos_to_camera[16];
+    float normal_to_camera[9];
+} cr_vertex_constants;
+
+/* The reference's vertexShader_gouraud (test/shader/Shaders.cu:55-82) with
+ * evaluateLighting (Shaders.cu:37-50). in_vertices: InputVertex records of 8
+ * floats (modelPos xyz, modelNormal xyz, texCoord uv); materials: num_materials
+ * records of 8 floats (diffuse rgba, specular rgb, glossiness -- the lighting
+ * fields of the reference's Material); vertex_material_idx: one index per
+ * vertex (clamped to the table); out_vertices: GouraudVertex records (clipPos,
+ * colour rgb + diffuse alpha). Arithmetic as the framework's C, one rounded
+ * operation at a time; sqrt is IEEE and powf an exactly specified power
+ * (cr_pow_exact) where the reference used fast-math approximations. Device
+ * pointers; asynchronous. No counterpart call in the reference's host code. */
+cr_status cr_vertex_shader_gouraud(const void* in_vertices, int64_t num_vertices,
+                                   const cr_vertex_constants* constants, const void* materials,
+                                   int32_t num_materials, const int32_t* vertex_material_idx,
+                                   void* out_vertices, void* stream);
+
+/* The reference's vertexShader_texPhong (test/shader/Shaders.cu:86-108):
+ * InputVertex records -> ShadedVertex_texPhong records of 16 floats (clipPos,
+ * cameraPos, cameraNormal with w 0, texCoord with z 0 and w 1). */
+cr_status cr_vertex_shader_tex_phong(const void* in_vertices, int64_t num_vertices,
+                                    const cr_vertex_constants* constants, void* out_vertices, void* stream);
+
+/* The exact power the Gouraud vertex shader uses: out[i] = x[i]^y[i] for
+ * x >= 0, within about 1e-5 relative of pow (device arrays; asynchronous). */
+cr_status cr_pow_exact(const float* x, const float* y, float* out, int64_t n, void* stream);
+
 /* ---- MSAA resolve ----
  * The reference's CudaSurface::resolveToScreen (CudaSurface.hpp:73) is
  * commented out and drew through GL. This averages each pixel's samples per
