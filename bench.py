@@ -204,14 +204,14 @@ def flythrough_oracle_check(ft, kept, f):
     layers, all host cores)."""
     import time
     from oracle import oracle as orc
-    raster = importlib.import_module(PKG + ".raster")
+    from oracle import vertex_oracle
     pkg = importlib.import_module(PKG)
     workloads = importlib.import_module(PKG + ".workloads")
     t0 = time.perf_counter()
     clear = (pkg.color_to_abgr(*workloads.WATER_CLEAR[:4]), pkg.clear_depth_from_float(workloads.WATER_CLEAR[4]))
     color = depth = None
     for k, layer in enumerate(ft.layers):
-        clip = raster.vertex_shader_reference(layer["model"].cpu().numpy(), ft.mvps[f])
+        clip = vertex_oracle.vertex_passthrough(layer["model"].cpu().numpy(), ft.mvps[f])
         verts = np.concatenate([clip, layer["colors"].cpu().numpy()], axis=1).astype(np.float32)
         p = orc.make_pipe(ft.width, ft.height, 1, orc.DEPTH | orc.LERP, "replace" if k == 0 else "srcover",
                           "gouraud", 32, clear if k == 0 else None)

@@ -100,7 +100,12 @@ _SIGNATURES = {
     "cr_vertex_shader_passthrough": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
                                                C.c_int64, C.POINTER(C.c_float), C.c_void_p]),
     "cr_vertex_shader_gouraud": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(VertexConstants), C.c_void_p, C.c_int32,
-                                           C.c_void_p, C.c_void_p, C.c_void_p]),
+                                           C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "cr_set_tex_phong_constants": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32,
+                                             C.c_int32, C.c_void_p]),
+    "cr_texture_sample": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    "cr_texture_sample_hw": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int64,
+                                       C.c_void_p]),
     "cr_vertex_shader_tex_phong": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(VertexConstants), C.c_void_p,
                                              C.c_void_p]),
     "cr_pow_exact": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),

@@ -387,17 +387,19 @@ def vertex_shader_gouraud(vertices: torch.Tensor, pos_to_clip, pos_to_camera, no
                           materials: torch.Tensor, material_idx: torch.Tensor, out: torch.Tensor | None = None,
                           stream: torch.cuda.Stream | None = None) -> torch.Tensor:
     """The reference's vertexShader_gouraud on the GPU. vertices: [N, 8] InputVertex
-    records (position, normal, texture coordinate); materials: [M, 8] (diffuse rgba,
-    specular rgb, glossiness); material_idx: [N] int32. Returns [N, 8] GouraudVertex
-    records (clip position, lit colour)."""
+    records (position, normal, texture coordinate); materials: [M, K] float32 rows, K >= 8,
+    starting with diffuse rgba, specular rgb, glossiness (K = 144 for the reference's
+    Material records); material_idx: [N] int32. Returns [N, 8] GouraudVertex records
+    (clip position, lit colour)."""
     lib = _lib.load()
     n = vertices.shape[0]
     if out is None:
         out = torch.empty((n, 8), dtype=torch.float32, device=vertices.device)
     k = _vertex_constants(pos_to_clip, pos_to_camera, normal_to_camera)
     s = (stream or torch.cuda.current_stream()).cuda_stream
-    check(lib.cr_vertex_shader_gouraud(vertices.data_ptr(), n, C.byref(k), materials.data_ptr(), materials.shape[0],
-                                       material_idx.data_ptr(), out.data_ptr(), C.c_void_p(s)))
+    check(lib.cr_vertex_shader_gouraud(vertices.data_ptr(), n, C.byref(k), materials.data_ptr(),
+                                       materials.shape[1] * 4, materials.shape[0], material_idx.data_ptr(),
+                                       out.data_ptr(), C.c_void_p(s)))
     return out
 
 
@@ -415,25 +417,61 @@ def vertex_shader_tex_phong(vertices: torch.Tensor, pos_to_clip, pos_to_camera, 
     return out
 
 
+MATERIAL_FLOATS = 144   # the reference's Material record (Shaders.hpp): 576 bytes
+
+
+def material_records(diffuse, specular, glossiness, diffuse_texture=None, alpha_texture=None):
+    """Packs materials into [M, 144] float32 Material records. diffuse: [M, 4]; specular:
+    [M, 3]; glossiness: [M]; *_texture: optional lists of None or (size_xy, mip_levels)
+    with mip_levels [L <= 16, 4] rows (scaleX, scaleY, biasX, biasY) into the atlas
+    (levels past L repeat the last)."""
+    import numpy as np
+    d = np.asarray(diffuse, np.float32).reshape(-1, 4)
+    m = np.zeros((d.shape[0], MATERIAL_FLOATS), np.float32)
+    m[:, 0:4] = d
+    m[:, 4:7] = np.asarray(specular, np.float32).reshape(-1, 3)
+    m[:, 7] = np.asarray(glossiness, np.float32).reshape(-1)
+    for base, texs in ((8, diffuse_texture), (76, alpha_texture)):
+        for i, t in enumerate(texs or []):
+            if t is None:
+                continue
+            size, levels = t
+            lv = np.asarray(levels, np.float32).reshape(-1, 4)
+            m[i, base:base + 2] = size
+            for k in range(16):
+                m[i, base + 4 + 4 * k: base + 8 + 4 * k] = lv[min(k, lv.shape[0] - 1)]
+    return m
+
+
+def set_tex_phong_constants(materials: torch.Tensor, triangle_material_idx: torch.Tensor, atlas: torch.Tensor,
+                            stream: torch.cuda.Stream | None = None) -> None:
+    """Inputs of the PixelPipe_texPhong* pipes (the reference's c_constants and
+    t_textureAtlas): materials [M, 144] float32 CUDA tensor of Material records, one
+    int32 material index per triangle, atlas [H, W] int32/uint32 RGBA8 texels (R in the
+    low byte). The tensors must stay alive while draws use them."""
+    s = (stream or torch.cuda.current_stream()).cuda_stream
+    check(_lib.load().cr_set_tex_phong_constants(materials.data_ptr(), materials.shape[0],
+                                                 triangle_material_idx.data_ptr(), triangle_material_idx.numel(),
+                                                 atlas.data_ptr(), atlas.shape[1], atlas.shape[0], C.c_void_p(s)))
+
+
+def texture_sample(atlas: torch.Tensor, uv: torch.Tensor, hardware: bool = False,
+                   stream: torch.cuda.Stream | None = None) -> torch.Tensor:
+    """The textured pipe's atlas filter at uv [N, 2] (float32 CUDA): [N, 4] channels in
+    [0, 1]. hardware=True runs the same lookups through the texture unit instead."""
+    out = torch.empty((uv.shape[0], 4), dtype=torch.float32, device=uv.device)
+    s = (stream or torch.cuda.current_stream()).cuda_stream
+    fn = _lib.load().cr_texture_sample_hw if hardware else _lib.load().cr_texture_sample
+    check(fn(atlas.data_ptr(), atlas.shape[1], atlas.shape[0], uv.data_ptr(), out.data_ptr(), uv.shape[0],
+             C.c_void_p(s)))
+    return out
+
+
 def pow_exact(x: torch.Tensor, y: torch.Tensor, stream: torch.cuda.Stream | None = None) -> torch.Tensor:
     """The vertex lighting's exact power, elementwise on float32 CUDA tensors."""
     out = torch.empty_like(x)
     s = (stream or torch.cuda.current_stream()).cuda_stream
     check(_lib.load().cr_pow_exact(x.data_ptr(), y.data_ptr(), out.data_ptr(), x.numel(), C.c_void_p(s)))
-    return out
-
-
-def vertex_shader_reference(model, mvp):
-    """Host restatement (numpy float32) of the same product, used by tests."""
-    import numpy as np
-    m = np.asarray(mvp, dtype=np.float32).reshape(4, 4)
-    v = np.asarray(model, dtype=np.float32)
-    out = np.empty((v.shape[0], 4), np.float32)
-    for r in range(4):
-        acc = np.zeros(v.shape[0], np.float32)
-        for c in range(3):
-            acc = acc + m[r, c] * v[:, c]
-        out[:, r] = acc + m[r, 3] * np.float32(1.0)
     return out
 
 

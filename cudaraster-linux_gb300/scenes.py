@@ -212,6 +212,87 @@ def terrain(n: int, width: int, height: int, samples: int = 1, seed: int = 0, fr
             "width": width, "height": height, "samples": samples, "mvp": mvp, "model": pos, "rgba": rgba}
 
 
+def _mip_chain(img: np.ndarray) -> list[np.ndarray]:
+    """Box-filtered mip levels of a square RGBA8 image [n, n, 4] (n a power of two)."""
+    levels = [img]
+    while levels[-1].shape[0] > 1:
+        a = levels[-1].astype(np.uint32)
+        b = (a[0::2, 0::2] + a[1::2, 0::2] + a[0::2, 1::2] + a[1::2, 1::2] + 2) // 4
+        levels.append(b.astype(np.uint8))
+    return levels
+
+
+def texture_atlas(textures: list[np.ndarray], atlas_w: int = 256, atlas_h: int = 256):
+    """Packs square RGBA8 textures and their mip chains into one atlas. Each texture
+    takes a 2n x n strip holding its levels side by side from the left, top-aligned.
+    Returns (atlas [H, W] uint32 with R in the low byte, [(size, mip_levels[L, 4])]) with
+    mip_levels in the Material layout (scaleX, scaleY, biasX, biasY, normalized to the
+    atlas)."""
+    atlas = np.zeros((atlas_h, atlas_w, 4), np.uint8)
+    specs, x0, y0, row_h = [], 0, 0, 0
+    for tex in textures:
+        n = tex.shape[0]
+        if x0 + 2 * n > atlas_w:
+            x0, y0 = 0, y0 + row_h
+            row_h = 0
+        assert y0 + n <= atlas_h, "atlas too small"
+        levels, x = [], x0
+        for k, lv in enumerate(_mip_chain(tex)):
+            m = lv.shape[0]
+            atlas[y0:y0 + m, x:x + m] = lv
+            levels.append((m / atlas_w, m / atlas_h, x / atlas_w, y0 / atlas_h))
+            x += m
+        specs.append(((float(n), float(n)), np.array(levels, np.float32)))
+        x0 += 2 * n
+        row_h = max(row_h, n)
+    words = atlas.astype(np.uint32)
+    packed = words[..., 0] | (words[..., 1] << 8) | (words[..., 2] << 16) | (words[..., 3] << 24)
+    return packed.astype(np.uint32), specs
+
+
+def textured_terrain(n: int = 128, width: int = 640, height: int = 480, seed: int = 0, frame: float = 0.0,
+                     tiles: float = 6.0) -> dict:
+    """The heightfield as InputVertex records (position, normal, texture coordinate) for the
+    textured Phong pipe, with four materials -- untextured; diffuse-textured; diffuse and
+    alpha textured (the alpha test cuts holes); a second diffuse texture -- assigned per
+    triangle, an atlas holding their mip chains, and the camera matrices."""
+    rng = np.random.default_rng(seed)
+    pos, _, tris = grid_mesh(n, seed)
+    hgt = pos[:, 1].reshape(n, n)
+    step = 2.0 / (n - 1)
+    gx = np.gradient(hgt, step, axis=1)
+    gz = np.gradient(hgt, step, axis=0)
+    nrm = np.stack([-gx, np.ones_like(gx), -gz], axis=-1).reshape(-1, 3)
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    uv = np.stack([(pos[:, 0] + 1.0) * 0.5 * tiles - tiles * 0.5, (pos[:, 2] + 1.0) * 0.5 * tiles], axis=-1)
+    inp = np.concatenate([pos, nrm, uv], axis=1).astype(np.float32)
+
+    def noise_tex(k, lo, hi):
+        t = np.stack([value_noise(64, 64, 4, seed + k + c) for c in range(4)], axis=-1)
+        t = (t - t.min()) / max(float(t.max() - t.min()), 1e-6)
+        return np.clip(lo + (hi - lo) * t + rng.uniform(-0.08, 0.08, t.shape), 0, 1)
+
+    texs = [(noise_tex(10, 0.1, 0.9) * 255).round().astype(np.uint8),
+            (noise_tex(20, 0.0, 1.0) * 255).round().astype(np.uint8),
+            (noise_tex(30, 0.2, 0.8) * 255).round().astype(np.uint8)]
+    atlas, specs = texture_atlas(texs, 256, 128)
+    from .raster import material_records
+    materials = material_records(
+        diffuse=[[0.7, 0.6, 0.5, 1.0], [1.0, 1.0, 1.0, 1.0], [1.0, 1.0, 1.0, 1.0], [1.0, 1.0, 1.0, 0.8]],
+        specular=[[0.3, 0.3, 0.3], [0.5, 0.5, 0.4], [0.2, 0.2, 0.2], [0.8, 0.8, 0.8]],
+        glossiness=[8.0, 32.0, 4.0, 96.0],
+        diffuse_texture=[None, specs[0], specs[2], specs[2]],
+        alpha_texture=[None, None, specs[1], None])
+    tri_mat = rng.integers(0, 4, tris.shape[0]).astype(np.int32)
+    eye, target = terrain_eye_target(frame, 25.0)
+    view = look_at(eye, target).astype(np.float32)
+    proj = perspective(60.0, width / height, 0.05, 10.0).astype(np.float32)
+    return {"name": f"textured{n}", "input": inp, "indices": tris, "width": width, "height": height,
+            "pos_to_clip": (proj @ view).astype(np.float32), "pos_to_camera": view,
+            "normal_to_camera": view[:3, :3].copy(), "materials": materials, "triangle_material_idx": tri_mat,
+            "atlas": atlas}
+
+
 BATCH_RESOLUTIONS = [(256, 256), (512, 512), (1024, 768), (1920, 1080)]
 
 

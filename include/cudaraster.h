@@ -232,8 +232,9 @@ typedef struct cr_vertex_constants {
 /* The reference's vertexShader_gouraud (test/shader/Shaders.cu:55-82) with
  * evaluateLighting (Shaders.cu:37-50). in_vertices: InputVertex records of 8
  * floats (modelPos xyz, modelNormal xyz, texCoord uv); materials: num_materials
- * records of 8 floats (diffuse rgba, specular rgb, glossiness -- the lighting
- * fields of the reference's Material); vertex_material_idx: one index per
+ * records material_stride_bytes apart (0 = 32) that start with diffuse rgba,
+ * specular rgb, glossiness -- the reference's Material (cr_material, 576
+ * bytes) or just its first 32 bytes; vertex_material_idx: one index per
  * vertex (clamped to the table); out_vertices: GouraudVertex records (clipPos,
  * colour rgb + diffuse alpha). Arithmetic as the framework's C, one rounded
  * operation at a time; sqrt is IEEE and powf an exactly specified power
@@ -241,14 +242,62 @@ typedef struct cr_vertex_constants {
  * pointers; asynchronous. No counterpart call in the reference's host code. */
 cr_status cr_vertex_shader_gouraud(const void* in_vertices, int64_t num_vertices,
                                    const cr_vertex_constants* constants, const void* materials,
-                                   int32_t num_materials, const int32_t* vertex_material_idx,
-                                   void* out_vertices, void* stream);
+                                   int32_t material_stride_bytes, int32_t num_materials,
+                                   const int32_t* vertex_material_idx, void* out_vertices, void* stream);
 
 /* The reference's vertexShader_texPhong (test/shader/Shaders.cu:86-108):
  * InputVertex records -> ShadedVertex_texPhong records of 16 floats (clipPos,
  * cameraPos, cameraNormal with w 0, texCoord with z 0 and w 1). */
 cr_status cr_vertex_shader_tex_phong(const void* in_vertices, int64_t num_vertices,
                                     const cr_vertex_constants* constants, void* out_vertices, void* stream);
+
+/* ---- Textured Phong pipe (PixelPipe_texPhong*) ----
+ * The reference's TextureSpec and Material (test/shader/Shaders.hpp), field
+ * for field: a texture's size in texels (0 = no texture) and per mip level
+ * (scaleX, scaleY, biasX, biasY) mapping [0, 1)^2 into the atlas. */
+typedef struct cr_texture_spec {
+    float size[2];
+    uint32_t pad[2];
+    float mip_levels[16][4];
+} cr_texture_spec;
+
+typedef struct cr_material {
+    float diffuse_color[4];
+    float specular_color[3];
+    float glossiness;
+    cr_texture_spec diffuse_texture;
+    cr_texture_spec alpha_texture;
+} cr_material;
+
+/* The fragment shader's inputs, which the reference kept in c_constants
+ * (materials, triangleMaterialIdx) and the texture reference t_textureAtlas:
+ * materials: device array of num_materials cr_material; triangle_material_idx:
+ * device array of num_triangle_material_idx indices, one per triangle of the
+ * draw (a triangle past the end uses the last entry; indices are clamped to
+ * the table); atlas: device RGBA8 texels (R in the low byte), atlas_width x
+ * atlas_height, sampled bilinearly with wrapped, normalized coordinates.
+ * Stream-ordered: draws on `stream` after this call read these values. One
+ * set is current at a time, as with the reference's module constants. */
+cr_status cr_set_tex_phong_constants(const cr_material* materials, int32_t num_materials,
+                                     const int32_t* triangle_material_idx, int64_t num_triangle_material_idx,
+                                     const uint32_t* atlas, int32_t atlas_width, int32_t atlas_height,
+                                     void* stream);
+
+/* The texture filter of the textured pipe over arrays: out[4 i + c] = channel c
+ * of the atlas filtered at (uv[2 i], uv[2 i + 1]) -- linear filtering, wrap
+ * addressing, normalized coordinates, 8-bit fractional weights rounded to
+ * nearest, the weighted integer sum divided by 255 * 65536 (the reference's
+ * tex2D on t_textureAtlas, test/shader/Shaders.cu:141-142, with its result
+ * specified). Device arrays; asynchronous. */
+cr_status cr_texture_sample(const uint32_t* atlas, int32_t atlas_width, int32_t atlas_height, const float* uv,
+                            float* out, int64_t n, void* stream);
+
+/* The same lookups through the GPU's texture unit (an RGBA8 CUDA array read as
+ * normalized floats, linear filter, wrap, normalized coordinates), for
+ * comparing cr_texture_sample with the hardware filter the reference used.
+ * Synchronises with `stream`. */
+cr_status cr_texture_sample_hw(const uint32_t* atlas, int32_t atlas_width, int32_t atlas_height, const float* uv,
+                               float* out, int64_t n, void* stream);
 
 /* The exact power the Gouraud vertex shader uses: out[i] = x[i]^y[i] for
  * x >= 0, within about 1e-5 relative of pow (device arrays; asynchronous). */

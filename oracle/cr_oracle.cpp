@@ -576,11 +576,224 @@ U32 trihash_color(S32 triIdx) {
     return h | 0xFF000000u;
 }
 
+// ---- Exactly specified shader arithmetic (the GPU's ShaderMath.hpp) ----
+// The reference's Shaders.cu calls log2f, powf, a reciprocal square root and
+// tex2D, whose results nvcc does not specify; the pipeline replaces them with
+// correctly rounded operations, restated here one operation at a time.
+inline F32 pow2i(int e) { U32 b = (U32)(e + 127) << 23; F32 f; std::memcpy(&f, &b, 4); return f; }
+inline U32 fbits(F32 f) { U32 b; std::memcpy(&b, &f, 4); return b; }
+inline F32 bitsf(U32 b) { F32 f; std::memcpy(&f, &b, 4); return f; }
+
+F32 log2_finite(F32 x) {  // finite x > 0: atanh series on the mantissa folded into [sqrt(1/2), sqrt(2)]
+    U32 b = fbits(x);
+    S32 k = 0;
+    if ((b >> 23) == 0u) { x = x * 16777216.0f; b = fbits(x); k = -24; }
+    k += (S32)(b >> 23) - 127;
+    F32 m = bitsf((b & 0x7FFFFFu) | 0x3F800000u);
+    if (m > 1.41421354f) { m = m * 0.5f; k += 1; }
+    const F32 t = (m - 1.0f) / (m + 1.0f);
+    const F32 t2 = t * t;
+    F32 p = 0.26230818f;
+    p = p * t2 + 0.3205989f;
+    p = p * t2 + 0.41219857f;
+    p = p * t2 + 0.57707804f;
+    p = p * t2 + 0.9617967f;
+    p = p * t2 + 2.88539f;
+    return (F32)k + t * p;
+}
+
+F32 log2_full(F32 x) {
+    if (x != x) return x;
+    if (x == 0.0f) return -INFINITY;
+    if (x < 0.0f) return NAN;
+    if (std::isinf(x)) return x;
+    return log2_finite(x);
+}
+
+F32 exp2_exact(F32 z) {  // 2^n * sqrt(2) * 2^f, 2^f by its Taylor series
+    if (z != z) return z;
+    if (z >= 128.0f) return INFINITY;
+    if (!(z > -150.0f)) return 0.0f;
+    const F32 n = std::floor(z);
+    const F32 f = (z - n) - 0.5f;
+    F32 p = 1.0178086e-07f;
+    p = p * f + 1.3215487e-06f;
+    p = p * f + 1.5252734e-05f;
+    p = p * f + 1.540353e-04f;
+    p = p * f + 1.3333558e-03f;
+    p = p * f + 9.618129e-03f;
+    p = p * f + 5.550411e-02f;
+    p = p * f + 2.402265e-01f;
+    p = p * f + 6.931472e-01f;
+    p = p * f + 1.0f;
+    p = p * 1.4142135f;
+    S32 ni = (S32)n;
+    if (ni < -126) { p = p * pow2i(-64); ni += 64; }
+    return p * pow2i(ni);
+}
+
+F32 pow_exact(F32 x, F32 y) {
+    if (y == 0.0f) return 1.0f;
+    if (!(x > 0.0f)) return y > 0.0f ? 0.0f : INFINITY;
+    if (std::isinf(x)) return y > 0.0f ? x : 0.0f;
+    return exp2_exact(y * log2_finite(x));
+}
+
+inline F32 dot3(const F32 a[3], const F32 b[3]) { return ((0.0f + a[0] * b[0]) + a[1] * b[1]) + a[2] * b[2]; }
+
+void normalize3(const F32 v[3], F32 r[3]) {  // v * (1 * rcp(length)), rcp(0) = 0
+    const F32 len = std::sqrt(dot3(v, v));
+    const F32 s = 1.0f * (len != 0.0f ? 1.0f / len : 0.0f);
+    for (int k = 0; k < 3; k++) r[k] = v[k] * s;
+}
+
+// test/shader/Shaders.cu:37-50 evaluateLighting.
+void evaluate_lighting(const F32 cameraPos[3], const F32 cameraNormal[3], const F32 spec[3], F32 gloss,
+                       const F32 diffuse[3], F32 out[3]) {
+    F32 I[3], N[3], R[3];
+    normalize3(cameraPos, I);
+    normalize3(cameraNormal, N);
+    const F32 dotIN = dot3(I, N);
+    const F32 twice = dotIN * 2.0f;
+    for (int k = 0; k < 3; k++) R[k] = I[k] - N[k] * twice;
+    const F32 diffuseCoef = std::fmax(-dotIN, 0.0f) * 0.75f + 0.25f;
+    const F32 specularCoef = pow_exact(std::fmax(-dot3(I, R), 0.0f), gloss);
+    for (int k = 0; k < 3; k++) out[k] = diffuseCoef * diffuse[k] + specularCoef * spec[k];
+}
+
+// Bilinear RGBA8 atlas lookup: wrap, normalized coordinates, 8-bit weights
+// rounded to nearest, integer weighted sum / (255 * 65536).
+void tex_axis(F32 u, S32 n, S32* i0, S32* i1, U32* w) {
+    F32 f = u - std::floor(u);
+    if (!(f >= 0.0f && f < 1.0f)) f = 0.0f;
+    const F32 x = f * (F32)n - 0.5f;
+    const F32 fl = std::floor(x);
+    const S32 i = (S32)fl;
+    *w = (U32)(S32)std::nearbyint((x - fl) * 256.0f);
+    *i0 = i < 0 ? i + n : (i >= n ? i - n : i);
+    *i1 = *i0 + 1 == n ? 0 : *i0 + 1;
+}
+
+void tex2d(const U32* atlas, S32 w, S32 h, F32 u, F32 v, F32 out[4]) {
+    S32 x0, x1, y0, y1;
+    U32 a, b;
+    tex_axis(u, w, &x0, &x1, &a);
+    tex_axis(v, h, &y0, &y1, &b);
+    const U32 c00 = atlas[(S64)y0 * w + x0], c10 = atlas[(S64)y0 * w + x1];
+    const U32 c01 = atlas[(S64)y1 * w + x0], c11 = atlas[(S64)y1 * w + x1];
+    const U32 w00 = (256u - a) * (256u - b), w10 = a * (256u - b), w01 = (256u - a) * b, w11 = a * b;
+    for (int k = 0; k < 4; k++) {
+        const int sh = 8 * k;
+        const U32 sum = w00 * ((c00 >> sh) & 255u) + w10 * ((c10 >> sh) & 255u) + w01 * ((c01 >> sh) & 255u) +
+                        w11 * ((c11 >> sh) & 255u);
+        out[k] = (F32)sum / 16711680.0f;
+    }
+}
+
+// The textured Phong shader's inputs (the reference's c_constants and
+// t_textureAtlas). Materials are the reference's 576-byte Material records.
+struct TexPhongEnv {
+    const F32* materials = nullptr;  // 144 floats each
+    int numMaterials = 0;
+    const int32_t* triMaterial = nullptr;
+    S64 numTriMaterial = 0;
+    const U32* atlas = nullptr;
+    S32 atlasW = 0, atlasH = 0;
+};
+TexPhongEnv g_texPhong;
+
+// Shaders.cu:123-147 texture2D; spec = the TextureSpec's 68 floats (size, pad, mip levels).
+void texture2d(const F32* spec, const F32 tex[2], const F32 texDX[2], const F32 texDY[2], F32 out[4]) {
+    const F32 sx = spec[0], sy = spec[1];
+    const F32 ax = texDX[0] * sx, ay = texDX[1] * sy, bx = texDY[0] * sx, by = texDY[1] * sy;
+    const F32 dxlen = ax * ax + ay * ay;
+    const F32 dylen = bx * bx + by * by;
+    const F32 lod = std::fmin(std::fmax(log2_full(std::fmax(dxlen, dylen)) * 0.5f, 0.0f), 14.0f);
+    const int levelIdx = (int)lod;
+    const F32* m0 = spec + 4 + 4 * levelIdx;
+    const F32* m1 = m0 + 4;
+    const F32 tx = tex[0] - std::floor(tex[0]);
+    const F32 ty = tex[1] - std::floor(tex[1]);
+    F32 v0[4], v1[4];
+    const TexPhongEnv& e = g_texPhong;
+    tex2d(e.atlas, e.atlasW, e.atlasH, tx * m0[0] + m0[2], ty * m0[1] + m0[3], v0);
+    tex2d(e.atlas, e.atlasW, e.atlasH, tx * m1[0] + m1[2], ty * m1[1] + m1[3], v1);
+    const F32 t = lod - (F32)levelIdx;
+    const F32 omt = 1.0f - t;
+    for (int k = 0; k < 4; k++) out[k] = v0[k] * omt + v1[k] * t;
+}
+
+// test/shader/Shaders.cu:149-193 FragmentShader_texPhong::run. Without quads
+// the texture is sampled at the centroid with its analytic derivatives; in
+// quad mode at the pixel centre, with dFdx / dFdy the differences of the
+// pixel-centre values across the 2x2 quad (right minus left in the row,
+// bottom minus top in the column).
+U32 shade_tex_phong(const ShadeCtx& c, const Data& d, S32 triIdx, S32 px, S32 py, const Barys& cb, bool* discard) {
+    F32 cp[4], cn[4], tex[2], texDX[2], texDY[2];
+    interpolate(c, d, 0, cb.c, cp);
+    interpolate(c, d, 1, cb.c, cn);
+    if (!(c.flags & OR_QUADS)) {
+        F32 t[4], tdx[4], tdy[4];
+        interpolate(c, d, 2, cb.c, t);
+        interpolate(c, d, 2, cb.dx, tdx);
+        interpolate(c, d, 2, cb.dy, tdy);
+        tex[0] = t[0]; tex[1] = t[1];
+        texDX[0] = tdx[0]; texDX[1] = tdx[1];
+        texDY[0] = tdy[0]; texDY[1] = tdy[1];
+    } else {
+        const S32 w[3] = {(S32)d.w[4], (S32)d.w[5], (S32)d.w[6]};
+        const S32 u[3] = {(S32)d.w[7], (S32)d.w[8], (S32)d.w[9]};
+        const S32 v[3] = {(S32)d.w[10], (S32)d.w[11], (S32)d.w[12]};
+        auto texAt = [&](S32 qx, S32 qy, F32 out[4]) {
+            Barys b = compute_barys(c.s, w, u, v, (qx * 2 + 1) << c.s, (qy * 2 + 1) << c.s);
+            interpolate(c, d, 2, b.c, out);
+        };
+        const S32 x0 = px & ~1, y0 = py & ~1;
+        F32 t[4], l[4], r[4], tp[4], bt[4];
+        texAt(px, py, t);
+        texAt(x0, py, l);
+        texAt(x0 + 1, py, r);
+        texAt(px, y0, tp);
+        texAt(px, y0 + 1, bt);
+        tex[0] = t[0]; tex[1] = t[1];
+        texDX[0] = r[0] - l[0]; texDX[1] = r[1] - l[1];
+        texDY[0] = bt[0] - tp[0]; texDY[1] = bt[1] - tp[1];
+    }
+    const TexPhongEnv& e = g_texPhong;
+    if (!e.materials || !e.triMaterial || !e.atlas || e.numMaterials < 1 || e.numTriMaterial < 1) {
+        *discard = true;  // no inputs set: as the GPU shader, nothing to read
+        return 0;
+    }
+    const S64 slot = std::min((S64)triIdx, e.numTriMaterial - 1);
+    const int materialIdx = std::min(std::max((int)e.triMaterial[slot], 0), e.numMaterials - 1);
+    const F32* m = e.materials + (S64)materialIdx * 144;
+    F32 diffuse[4] = {m[0], m[1], m[2], m[3]};
+    const F32* diffuseTexture = m + 8;
+    const F32* alphaTexture = m + 76;
+    F32 tc[4];
+    if (diffuseTexture[0] != 0.0f) {
+        texture2d(diffuseTexture, tex, texDX, texDY, tc);
+        diffuse[0] = tc[0]; diffuse[1] = tc[1]; diffuse[2] = tc[2];
+    }
+    if (alphaTexture[0] != 0.0f) {
+        texture2d(alphaTexture, tex, texDX, texDY, tc);
+        diffuse[3] = tc[1];
+    }
+    if (diffuse[3] < 0.5f) {
+        *discard = true;
+        return 0;
+    }
+    F32 color[3];
+    evaluate_lighting(cp, cn, m + 4, m[7], diffuse, color);
+    return to_abgr(color[0], color[1], color[2], diffuse[3]);
+}
+
 // FineRaster.inl:48-119 runFragmentShader, for the shaders the oracle knows.
 U32 shade(const ShadeCtx& c, const Data& d, S32 triIdx, S32 px, S32 py, U32 centroid, bool* discard) {
     *discard = false;
     F32 center[3] = {0.0f, 0.0f, 1.0f}, centroidB[3] = {0.0f, 0.0f, 1.0f};
-    Barys bc{};
+    Barys bc{}, cb{};  // at the pixel centre, at the centroid (with derivatives)
+    cb.c[2] = 1.0f;
     if (c.flags & OR_LERP) {
         const S32 w[3] = {(S32)d.w[4], (S32)d.w[5], (S32)d.w[6]};
         const S32 u[3] = {(S32)d.w[7], (S32)d.w[8], (S32)d.w[9]};
@@ -588,12 +801,12 @@ U32 shade(const ShadeCtx& c, const Data& d, S32 triIdx, S32 px, S32 py, U32 cent
         bc = compute_barys(c.s, w, u, v, (px * 2 + 1) << c.s, (py * 2 + 1) << c.s);
         std::memcpy(center, bc.c, sizeof(center));
         if (c.s == 0) {
-            std::memcpy(centroidB, bc.c, sizeof(centroidB));
+            cb = bc;
         } else {
-            Barys bt = compute_barys(c.s, w, u, v, (px << (c.s + 1)) + (S32)(centroid & 0xF),
-                                     (py << (c.s + 1)) + (S32)(centroid >> 4));
-            std::memcpy(centroidB, bt.c, sizeof(centroidB));
+            cb = compute_barys(c.s, w, u, v, (px << (c.s + 1)) + (S32)(centroid & 0xF),
+                               (py << (c.s + 1)) + (S32)(centroid >> 4));
         }
+        std::memcpy(centroidB, cb.c, sizeof(centroidB));
     }
     switch (c.shader) {
     case OR_SHADER_GOURAUD: {
@@ -605,6 +818,8 @@ U32 shade(const ShadeCtx& c, const Data& d, S32 triIdx, S32 px, S32 py, U32 cent
         return to_abgr(1.0f, 0.0f, 0.0f, 1.0f);
     case OR_SHADER_TRIHASH:
         return trihash_color(triIdx);
+    case OR_SHADER_TEXPHONG:
+        return shade_tex_phong(c, d, triIdx, px, py, cb, discard);
     default:
         return to_abgr(bc.dx[1] * 64.0f, bc.dy[1] * 64.0f, center[2], 1.0f);
     }
@@ -963,6 +1178,30 @@ int or_find_bit(uint64_t mask, int idx, int quads) {
         if (mask >> b & 1) { if (idx == 0) return b; idx--; }
     return -1;
 }
+void or_set_tex_phong(const float* materials, int num_materials, const int32_t* triangle_material_idx,
+                      int64_t num_triangle_material_idx, const uint32_t* atlas, int atlas_width, int atlas_height) {
+    g_texPhong.materials = materials;
+    g_texPhong.numMaterials = num_materials;
+    g_texPhong.triMaterial = triangle_material_idx;
+    g_texPhong.numTriMaterial = num_triangle_material_idx;
+    g_texPhong.atlas = atlas;
+    g_texPhong.atlasW = atlas_width;
+    g_texPhong.atlasH = atlas_height;
+}
+
+void or_texture_sample(const uint32_t* atlas, int atlas_width, int atlas_height, const float* uv, float* out,
+                       int64_t n) {
+    for (int64_t i = 0; i < n; i++) tex2d(atlas, atlas_width, atlas_height, uv[2 * i], uv[2 * i + 1], out + 4 * i);
+}
+
+float or_pow_exact(float x, float y) { return pow_exact(x, y); }
+float or_log2_exact(float x) { return log2_full(x); }
+
+void or_evaluate_lighting(const float camera_pos[3], const float camera_normal[3], const float specular[3],
+                          float glossiness, const float diffuse[3], float out[3]) {
+    evaluate_lighting(camera_pos, camera_normal, specular, glossiness, diffuse, out);
+}
+
 uint32_t or_fragment(const or_pipe* p, const uint32_t data16[16], const float* vertices,
                      int32_t tri_idx, int32_t px, int32_t py, uint32_t centroid) {
     ShadeCtx c{vertices, p->vertex_stride / 16, p->samples_log2, p->render_mode, p->shader};

@@ -44,6 +44,7 @@ extern "C" {
 #define OR_SHADER_RED         1 /* constant red, test/shader/PassThrough.cu:44-54          */
 #define OR_SHADER_TRIHASH     2 /* ABGR from a hash of the triangle index (ordering probe)  */
 #define OR_SHADER_DERIV       3 /* colour from barycentric derivatives (quad mode probe)    */
+#define OR_SHADER_TEXPHONG    4 /* test/shader/Shaders.cu:117-193, inputs from or_set_tex_phong */
 
 typedef struct or_pipe {
     int32_t  width, height;       /* viewport = surface size in pixels            */
@@ -110,6 +111,21 @@ uint32_t or_triangle_sample_coverage(const uint32_t header[4], int px, int py,
 void     or_compute_barys(int samples_log2, const int32_t w[3], const int32_t u[3],
                           const int32_t v[3], int32_t sx, int32_t sy, float out[9]);
 int      or_find_bit(uint64_t mask, int idx, int quads);
+/* Inputs of the textured Phong shader (the reference's c_constants and
+ * t_textureAtlas): materials as 576-byte Material records (144 floats), one
+ * material index per triangle, an RGBA8 atlas. The pointers are kept, not
+ * copied, until the next call. */
+void     or_set_tex_phong(const float* materials, int num_materials, const int32_t* triangle_material_idx,
+                          int64_t num_triangle_material_idx, const uint32_t* atlas, int atlas_width,
+                          int atlas_height);
+/* The atlas filter (bilinear, wrap, normalized coordinates, 8-bit weights). */
+void     or_texture_sample(const uint32_t* atlas, int atlas_width, int atlas_height, const float* uv,
+                           float* out, int64_t n);
+/* The exactly specified power / log2 and evaluateLighting (Shaders.cu:37-50). */
+float    or_pow_exact(float x, float y);
+float    or_log2_exact(float x);
+void     or_evaluate_lighting(const float camera_pos[3], const float camera_normal[3], const float specular[3],
+                              float glossiness, const float diffuse[3], float out[3]);
 /* Fragment shader of pipe p for one pixel (FineRaster.inl:48-119). */
 uint32_t or_fragment(const or_pipe* p, const uint32_t data16[16], const float* vertices,
                      int32_t tri_idx, int32_t px, int32_t py, uint32_t centroid);

@@ -17,7 +17,7 @@ REF_LIB = HERE / "_ref" / "libcrref.so"
 
 DEPTH, LERP, QUADS = 1, 2, 4
 BLENDS = {"replace": 0, "srcover": 1, "additive": 2, "depthonly": 3}
-SHADERS = {"gouraud": 0, "red": 1, "trihash": 2, "deriv": 3}
+SHADERS = {"gouraud": 0, "red": 1, "trihash": 2, "deriv": 3, "texphong": 4}
 
 
 class Pipe(C.Structure):
@@ -70,6 +70,11 @@ def load():
             ("or_f32_to_s32_sat", C.c_int32, [C.c_float]), ("or_f32_to_u32_sat", C.c_uint32, [C.c_float]),
             ("or_f32_to_u32_sat_rmi", C.c_uint32, [C.c_float]), ("or_f32_to_s64", C.c_int64, [C.c_float]),
             ("or_f32_to_u32_rz", C.c_uint32, [C.c_float]),
+            ("or_set_tex_phong", None, [C.c_void_p, C.c_int, C.c_void_p, C.c_int64, C.c_void_p, C.c_int, C.c_int]),
+            ("or_texture_sample", None, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int64]),
+            ("or_pow_exact", C.c_float, [C.c_float, C.c_float]),
+            ("or_log2_exact", C.c_float, [C.c_float]),
+            ("or_evaluate_lighting", None, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p]),
         ]:
             fn = getattr(lib, name)
             fn.restype = res
@@ -124,6 +129,47 @@ def setup(pipe: Pipe, vertices: np.ndarray, indices: np.ndarray, max_subtris: in
     used = lib.or_setup(C.byref(pipe), v.ctypes.data, i.ctypes.data, t, sub.ctypes.data, hdr.ctypes.data,
                         dat.ctypes.data, ms)
     return sub, hdr, dat, used
+
+
+_tex_phong_keep = None
+
+
+def set_tex_phong(materials: np.ndarray, triangle_material_idx: np.ndarray, atlas: np.ndarray) -> None:
+    """Inputs of the textured Phong shader: materials [M, 144] float32 (576-byte Material
+    records), one int32 material index per triangle, an RGBA8 atlas [H, W] uint32."""
+    global _tex_phong_keep
+    lib = load()
+    m = np.ascontiguousarray(materials, dtype=np.float32).reshape(-1, 144)
+    t = np.ascontiguousarray(triangle_material_idx, dtype=np.int32).reshape(-1)
+    a = np.ascontiguousarray(atlas, dtype=np.uint32)
+    _tex_phong_keep = (m, t, a)
+    lib.or_set_tex_phong(m.ctypes.data, m.shape[0], t.ctypes.data, t.shape[0], a.ctypes.data, a.shape[1], a.shape[0])
+
+
+def texture_sample(atlas: np.ndarray, uv: np.ndarray) -> np.ndarray:
+    """The atlas filter at uv [N, 2]: [N, 4] float32 channels."""
+    lib = load()
+    a = np.ascontiguousarray(atlas, dtype=np.uint32)
+    p = np.ascontiguousarray(uv, dtype=np.float32).reshape(-1, 2)
+    out = np.zeros((p.shape[0], 4), np.float32)
+    lib.or_texture_sample(a.ctypes.data, a.shape[1], a.shape[0], p.ctypes.data, out.ctypes.data, p.shape[0])
+    return out
+
+
+def pow_exact(x: float, y: float) -> float:
+    return load().or_pow_exact(x, y)
+
+
+def log2_exact(x: float) -> float:
+    return load().or_log2_exact(x)
+
+
+def evaluate_lighting(camera_pos, camera_normal, specular, glossiness, diffuse) -> np.ndarray:
+    arrs = [np.ascontiguousarray(v, dtype=np.float32) for v in (camera_pos, camera_normal, specular, diffuse)]
+    out = np.zeros(3, np.float32)
+    load().or_evaluate_lighting(arrs[0].ctypes.data, arrs[1].ctypes.data, arrs[2].ctypes.data, float(glossiness),
+                                arrs[3].ctypes.data, out.ctypes.data)
+    return out
 
 
 def ref_available() -> bool:

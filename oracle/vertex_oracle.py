@@ -125,6 +125,20 @@ def _normalize3(v: np.ndarray) -> np.ndarray:
     return (v * s[:, None]).astype(np.float32)
 
 
+def vertex_passthrough(model, mvp) -> np.ndarray:
+    """vertexShader_passthrough (test/shader/PassThrough.cu:16-35): clip = MVP * (xyz, 1),
+    each row summed left to right from zero (Math.hpp:990-1001)."""
+    m = np.asarray(mvp, dtype=np.float32).reshape(4, 4)
+    v = np.asarray(model, dtype=np.float32)
+    out = np.empty((v.shape[0], 4), np.float32)
+    for r in range(4):
+        acc = np.zeros(v.shape[0], np.float32)
+        for c in range(3):
+            acc = acc + m[r, c] * v[:, c]
+        out[:, r] = acc + m[r, 3] * np.float32(1.0)
+    return out
+
+
 def vertex_gouraud(vertices, pos_to_clip, pos_to_camera, normal_to_camera, materials, material_idx):
     """InputVertex records [N, 8] -> GouraudVertex records [N, 8]."""
     v = np.asarray(vertices, np.float32)

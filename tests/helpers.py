@@ -26,9 +26,14 @@ PIPES = {
     "PixelPipe_gouraud_msaa8": (orc.DEPTH | orc.LERP, "replace", "gouraud", 32),
     "PixelPipe_gouraud_srcover_msaa4": (orc.DEPTH | orc.LERP, "srcover", "gouraud", 32),
     "PixelPipe_trihash_srcover_msaa4": (0, "srcover", "trihash", 32),
+    "PixelPipe_texPhong": (orc.DEPTH | orc.LERP, "replace", "texphong", 64),
+    "PixelPipe_texPhong_quads": (orc.DEPTH | orc.LERP | orc.QUADS, "replace", "texphong", 64),
+    "PixelPipe_texPhong_srcover": (orc.DEPTH | orc.LERP, "srcover", "texphong", 64),
+    "PixelPipe_texPhong_msaa4": (orc.DEPTH | orc.LERP, "replace", "texphong", 64),
 }
 PIPE_SAMPLES = {"PixelPipe_gouraud_msaa2": 2, "PixelPipe_gouraud_msaa4": 4, "PixelPipe_gouraud_msaa8": 8,
-                "PixelPipe_gouraud_srcover_msaa4": 4, "PixelPipe_trihash_srcover_msaa4": 4}
+                "PixelPipe_gouraud_srcover_msaa4": 4, "PixelPipe_trihash_srcover_msaa4": 4,
+                "PixelPipe_texPhong_msaa4": 4}
 
 
 def pkg():
@@ -37,6 +42,8 @@ def pkg():
 
 def vertices_for(pipe: str, verts: np.ndarray) -> np.ndarray:
     stride = PIPES[pipe][3]
+    # The pipe reads stride bytes per vertex: a narrower array would be read past its end.
+    assert verts.ndim == 2 and verts.shape[1] * 4 >= stride, f"{pipe} needs {stride}-byte vertex records"
     return np.ascontiguousarray(verts[:, : stride // 4], dtype=np.float32)
 
 

@@ -13,6 +13,7 @@ import torch
 
 from conftest import pkg_mod
 from helpers import assert_same, oracle_render, pkg
+from oracle import vertex_oracle
 
 pytestmark = pytest.mark.gpu
 
@@ -68,7 +69,7 @@ def test_flythrough_frame_matches_oracle(fly, plain):
     clear = (p.color_to_abgr(*wl.WATER_CLEAR[:4]), p.clear_depth_from_float(wl.WATER_CLEAR[4]))
     color = depth = None
     for k, (layer, pipe) in enumerate(zip(fly.layers, ("PixelPipe_gouraud", "PixelPipe_gouraud_srcover"))):
-        clip = raster.vertex_shader_reference(layer["model"].cpu().numpy(), mvp)
+        clip = vertex_oracle.vertex_passthrough(layer["model"].cpu().numpy(), mvp)
         verts = np.concatenate([clip, layer["colors"].cpu().numpy()], axis=1).astype(np.float32)
         sc = {"vertices": verts, "indices": layer["indices"].cpu().numpy(), "width": W, "height": H}
         color, depth, st = oracle_render(pipe, sc, clear if k == 0 else None, color, depth)

@@ -24,7 +24,9 @@ def test_cube_config1(cuda):
     assert (rc != clear[0]).sum() > 100000
 
 
-@pytest.mark.parametrize("pipe", [p for p in PIPES if p not in PIPE_SAMPLES and p != "PixelPipe_deriv_quads"])
+# Pipes that draw the soup's GouraudVertex records (the textured pipes have their own tests).
+@pytest.mark.parametrize("pipe", [p for p in PIPES if p not in PIPE_SAMPLES and p != "PixelPipe_deriv_quads"
+                                  and PIPES[p][3] <= 32])
 def test_soup_pipes(cuda, pipe):
     sc = pkg_mod("scenes").soup(20000, 320, 240, seed=11, median_px=6.0)
     clear = clear_of()
@@ -54,7 +56,7 @@ def test_quad_derivatives_cube(cuda):
     assert_same(gc, gd, rc, rd, "deriv quads cube")
 
 
-@pytest.mark.parametrize("pipe", list(PIPE_SAMPLES))
+@pytest.mark.parametrize("pipe", [p for p in PIPE_SAMPLES if PIPES[p][3] <= 32])
 def test_soup_msaa(cuda, pipe):
     sc = pkg_mod("scenes").soup(8000, 200, 136, seed=5, median_px=5.0)
     sc["samples"] = PIPE_SAMPLES[pipe]

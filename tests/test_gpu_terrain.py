@@ -8,6 +8,7 @@ import torch
 
 from conftest import pkg_mod
 from helpers import assert_same, gpu_render, oracle_render, pkg
+from oracle import vertex_oracle
 
 pytestmark = pytest.mark.gpu
 
@@ -26,7 +27,7 @@ def test_vertex_shader_bit_exact(cuda):
     out = raster.vertex_shader_passthrough(torch.from_numpy(model).cuda(), mvp, torch.from_numpy(colors).cuda())
     torch.cuda.synchronize()
     got = out.cpu().numpy()
-    ref = raster.vertex_shader_reference(model, mvp)
+    ref = vertex_oracle.vertex_passthrough(model, mvp)
     np.testing.assert_array_equal(got[:, :4].view(np.uint32), ref.view(np.uint32))
     np.testing.assert_array_equal(got[:, 4:], colors)
 
@@ -39,7 +40,7 @@ def _terrain(n, w, h, samples, frame):
     model = pos.astype(np.float32)
     clip_gpu = raster.vertex_shader_passthrough(torch.from_numpy(model).cuda(), mvp,
                                                 torch.from_numpy(rgba).cuda()).cpu().numpy()
-    clip_ref = raster.vertex_shader_reference(model, mvp)
+    clip_ref = vertex_oracle.vertex_passthrough(model, mvp)
     assert (clip_gpu[:, :4].view(np.uint32) == clip_ref.view(np.uint32)).all()
     return {"vertices": clip_gpu, "indices": tris, "width": w, "height": h, "samples": samples}
 
