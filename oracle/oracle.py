@@ -212,4 +212,10 @@ def load_ref():
     lib.ref_encode_depth.argtypes = [C.c_uint]
     lib.ref_decode_depth.argtypes = [C.c_uint]
     lib.ref_select_flips.argtypes = [C.c_int, C.c_int]
+    lib.ref_vertex_gouraud.argtypes = [C.c_void_p, C.c_int] + [C.c_void_p] * 6
+    lib.ref_vertex_tex_phong.argtypes = [C.c_void_p, C.c_int] + [C.c_void_p] * 4
+    lib.ref_set_tex_phong.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int]
+    lib.ref_tex_phong_fragment.restype = C.c_uint
+    lib.ref_tex_phong_fragment.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_uint,
+                                           C.POINTER(C.c_int)]
     return lib

@@ -10,6 +10,11 @@ Fixtures (npz, seeded inputs + the reference's outputs):
   ref_coverage.npz  8x8 pixel coverage (exact LUT path and conservative), MSAA sample coverage
   ref_shading.npz   toABGR, host toABGR, blends, barycentrics, Gouraud fragments, centroid LUTs
   ref_misc.npz      encodeDepth/decodeDepth, selectFlips, perspective matrices, clipping
+  ref_shaders.npz   the example shaders of test/shader/Shaders.cu: Gouraud and texPhong vertex
+                    shaders, FragmentShader_texPhong fragments (1 and 4 samples), with log2f /
+                    powf / tex2D bound to the pipeline's specified versions (oracle/ref_shaders.cpp)
+
+`python tests/golden/make_golden.py shaders` writes ref_shaders.npz alone.
 """
 from __future__ import annotations
 
@@ -56,10 +61,56 @@ def run_setup(ref, sc, s, flags, stride=32):
     return sub, hdr[:used], dat[:used]
 
 
+def shaders(ref):
+    """Vertex and texPhong fragment shaders of the reference, on the textured heightfield."""
+    rng = np.random.default_rng(20261204)
+    sc = scenes.textured_terrain(32, 320, 240, seed=3)
+    inp = np.ascontiguousarray(sc["input"], np.float32)
+    n = inp.shape[0]
+    k = [np.ascontiguousarray(sc[x], np.float32) for x in ("pos_to_clip", "pos_to_camera", "normal_to_camera")]
+    mats = np.ascontiguousarray(sc["materials"], np.float32)
+    vidx = rng.integers(0, mats.shape[0], n).astype(np.int32)
+    gouraud = np.zeros((n, 8), np.float32)
+    ref.ref_vertex_gouraud(P(inp), n, P(k[0]), P(k[1]), P(k[2]), P(mats), P(vidx), P(gouraud))
+    tex_phong = np.zeros((n, 16), np.float32)
+    ref.ref_vertex_tex_phong(P(inp), n, P(k[0]), P(k[1]), P(k[2]), P(tex_phong))
+    tri = np.ascontiguousarray(sc["triangle_material_idx"], np.int32)
+    atlas = np.ascontiguousarray(sc["atlas"], np.uint32)
+    ref.ref_set_tex_phong(P(mats), P(tri), P(atlas), atlas.shape[1], atlas.shape[0])
+    frag = {}
+    for s in (0, 2):
+        pipe = orc.make_pipe(320, 240, 1 << s, orc.DEPTH | orc.LERP, "replace", "texphong", 64)
+        _, _, dat, used = orc.setup(pipe, tex_phong, sc["indices"])
+        m = 2000
+        slots = rng.integers(0, used, m)
+        args = np.zeros((m, 4), np.int32)   # slot, px, py, centroid
+        col = np.zeros(m, np.uint32)
+        disc = np.zeros(m, np.int32)
+        for j, slot in enumerate(slots):
+            d16 = np.ascontiguousarray(dat[slot])
+            px, py = int(rng.integers(0, 320)), int(rng.integers(0, 240))
+            cen = (int(rng.integers(0, 2 << s)) | (int(rng.integers(0, 2 << s)) << 4)) if s else 0
+            dd = C.c_int(0)
+            col[j] = ref.ref_tex_phong_fragment(s, P(d16), P(tex_phong), int(slot), px, py, cen, C.byref(dd))
+            disc[j] = dd.value
+            args[j] = (slot, px, py, cen)
+        frag[f"s{s}_data"] = dat[:used]
+        frag[f"s{s}_args"] = args
+        frag[f"s{s}_color"] = col
+        frag[f"s{s}_discard"] = disc
+    np.savez_compressed(HERE / "ref_shaders.npz", input=inp, pos_to_clip=k[0], pos_to_camera=k[1],
+                        normal_to_camera=k[2], materials=mats, vertex_material_idx=vidx, gouraud=gouraud,
+                        tex_phong=tex_phong, triangle_material_idx=tri, atlas=atlas, **frag)
+
+
 def main():
     if not orc.ref_available():
         sys.exit("oracle/_ref/libcrref.so is missing: run `make -C oracle ref` where the reference sources are")
     ref = orc.load_ref()
+    if sys.argv[1:] == ["shaders"]:
+        shaders(ref)
+        print("ref_shaders.npz written to", HERE)
+        return
     rng = np.random.default_rng(20261203)
 
     # ---- setup
@@ -214,6 +265,7 @@ def main():
     np.savez_compressed(HERE / "ref_misc.npz", depth_in=dvals, depth_enc=enc, depth_dec=dec, flips_in=fl,
                         flips=flips, persp_args=persp_args, persp=persp, clip_in=clip_in, clip_out=clip_out,
                         clip_n=clip_n)
+    shaders(ref)
     print("golden fixtures written to", HERE)
 
 

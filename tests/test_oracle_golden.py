@@ -172,3 +172,35 @@ def test_oracle_setup_against_live_reference_random(lib):
             sub, hdr, dat, oused = orc.setup(orc.make_pipe(500, 300, 1 << s, f), v, idx)
             assert used == oused
             np.testing.assert_array_equal(sub, rsub)
+
+
+def test_vertex_shaders_match_reference():
+    # Shaders.cu:56-108 compiled from the reference's source, powf bound to the specified power.
+    from oracle import vertex_oracle as vo
+    z = _load("ref_shaders.npz")
+    k = [z["pos_to_clip"], z["pos_to_camera"], z["normal_to_camera"]]
+    g = vo.vertex_gouraud(z["input"], *k, z["materials"], z["vertex_material_idx"])
+    assert np.array_equal(g.view(np.uint32), z["gouraud"].view(np.uint32))
+    t = vo.vertex_tex_phong(z["input"], *k)
+    assert np.array_equal(t.view(np.uint32), z["tex_phong"].view(np.uint32))
+
+
+@pytest.mark.parametrize("s", [0, 2])
+def test_tex_phong_fragments_match_reference(lib, s):
+    # FragmentShader_texPhong::run (Shaders.cu:149-193) from the reference's source, with
+    # log2f / powf / tex2D bound to the specified versions; discards included.
+    z = _load("ref_shaders.npz")
+    orc.set_tex_phong(z["materials"], z["triangle_material_idx"], z["atlas"])
+    pipe = orc.make_pipe(320, 240, 1 << s, orc.DEPTH | orc.LERP, "replace", "texphong", 64)
+    verts = np.ascontiguousarray(z["tex_phong"])
+    dat = z[f"s{s}_data"]
+    discards = 0
+    for (slot, px, py, cen), col, disc in zip(z[f"s{s}_args"], z[f"s{s}_color"], z[f"s{s}_discard"]):
+        d16 = np.ascontiguousarray(dat[slot])
+        got = lib.or_fragment(C.byref(pipe), P(d16), P(verts), int(slot), int(px), int(py), int(cen))
+        if disc:
+            discards += 1
+            assert got == 0          # the oracle returns 0 for a discarded fragment
+        else:
+            assert got == col
+    assert 0 < discards < len(z[f"s{s}_color"])
