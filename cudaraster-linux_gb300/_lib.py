@@ -81,6 +81,7 @@ _SIGNATURES = {
     "cr_deferred_clear_raw": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32]),
     "cr_set_pixel_pipe": (C.c_int, [C.c_void_p, C.c_char_p]),
     "cr_set_vertex_buffer": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
+    "cr_set_vertex_transform": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
     "cr_set_index_buffer": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32]),
     "cr_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
     "cr_set_debug_params": (C.c_int, [C.c_void_p, C.POINTER(DebugParams)]),

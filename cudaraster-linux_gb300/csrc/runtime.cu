@@ -111,6 +111,10 @@ struct cr_context {
     const void* indices = nullptr;
     int numTris = 0;
     bool vertexSet = false, indexSet = false;
+    // Fused vertex transform (cr_set_vertex_transform).
+    const float* model = nullptr;
+    int modelStride = 0;
+    float mvp[16] = {};
     cr_tuning tuning{};
     // Capacities (elements), grown by the rerun loop and kept across draws.
     int64_t maxSubtris = 0, maxBinEntries = 0, maxTileEntries = 0;
@@ -339,6 +343,23 @@ cr_status cr_set_vertex_buffer(cr_context* ctx, const void* vertices, int64_t of
     return CR_OK;
 }
 
+cr_status cr_set_vertex_transform(cr_context* ctx, const float* model, int32_t model_stride,
+                                  const float* mvp_row_major) {
+    if (!ctx) return CR_ERR_INVALID_ARGUMENT;
+    if (!model) {
+        ctx->model = nullptr;
+        ctx->modelStride = 0;
+        return CR_OK;
+    }
+    if (!mvp_row_major || model_stride < 3 || ((uintptr_t)model & 3))
+        return fail(ctx, CR_ERR_INVALID_ARGUMENT, "CudaRaster: bad vertex transform (model stride >= 3 floats, "
+                                                  "4-byte aligned, 16 matrix entries)");
+    ctx->model = model;
+    ctx->modelStride = model_stride;
+    memcpy(ctx->mvp, mvp_row_major, sizeof(ctx->mvp));
+    return CR_OK;
+}
+
 cr_status cr_set_index_buffer(cr_context* ctx, const void* indices, int64_t offset_bytes, int32_t num_tris) {
     if (!ctx) return CR_ERR_INVALID_ARGUMENT;
     if (!indices) {
@@ -405,6 +426,10 @@ struct Plan {
     int64_t totalTris = 0, chunkCountEntries = 0;
     int32_t totalBins = 0, totalTiles = 0, totalChunks = 0, maxBins = 0;
     int binLog2 = 4, unitEntries = 0;
+    // Fused vertex transform (single draws only).
+    const float* model = nullptr;
+    int modelStride = 0;
+    float mvp[16] = {};
 };
 
 // Coarse units a draw may use. A unit size set by the caller bounds them by
@@ -564,6 +589,10 @@ DrawDev makeDrawDev(cr_context* ctx, const Plan& plan) {
     d.totalChunks = plan.totalChunks;
     d.unitEntries = plan.unitEntries;
     d.totalTris = plan.totalTris;
+    d.model = plan.model;
+    d.modelStride = plan.modelStride;
+    d.modelVec4 = plan.model && plan.modelStride == 4 && ((uintptr_t)plan.model & 15) == 0;
+    memcpy(d.mvp, plan.mvp, sizeof(d.mvp));
     d.triSubtris = ctx->triSubtris.as<uint8_t>();
     d.triHeader = ctx->triHeader.as<uint4>();
     d.triData = ctx->triData.as<uint4>();
@@ -725,6 +754,11 @@ cr_status drawCurrent(cr_context* ctx, void* stream, bool sync) {
     std::vector<HostInstance> v{h};
     cr_status st = buildPlan(ctx, v, plan);
     if (st != CR_OK) return st;
+    if (ctx->model) {
+        plan.model = ctx->model;
+        plan.modelStride = ctx->modelStride;
+        memcpy(plan.mvp, ctx->mvp, sizeof(plan.mvp));
+    }
     st = drawPlan(ctx, plan, (cudaStream_t)stream, sync);
     if (st == CR_OK) ctx->deferredClear = false;  // CudaRaster.cpp:341
     return st;

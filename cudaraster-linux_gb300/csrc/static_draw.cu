@@ -215,6 +215,9 @@ extern "C" cr_status cr_draw_triangles_static(const char* pipe_name, void* color
     d.chunkBinOffset = (int32_t*)(scratch + kOffChunkOffset);
     d.maxBins = numBins;
     d.fineSelfPixels = 0;
+    d.model = nullptr;
+    d.modelStride = 0;
+    d.modelVec4 = 0;
     d.binCount = (int32_t*)(scratch + kOffBinCount);
     d.binStart = (int32_t*)(scratch + kOffBinStart);
     d.binUnitFirst = (int32_t*)(scratch + kOffBinUnitFirst);

@@ -220,6 +220,20 @@ class CudaRaster:
         self._vb = buf
         self._check(self._lib.cr_set_vertex_buffer(self._ctx, ptr, int(ofs)))
 
+    def setVertexTransform(self, model: torch.Tensor | None, mvp=None) -> None:
+        """Fuses vertexShader_passthrough into setup: while set, drawTriangles takes each
+        vertex's clip position as mvp * (model[i, :3], 1) (same bits as running the shader
+        first) and reads only the varyings from the vertex buffer. model: [N, >=3] float32
+        CUDA tensor (kept alive here); mvp: 16 values, row-major. None turns it off."""
+        self._need_init()
+        if model is None:
+            self._model = None
+            self._check(self._lib.cr_set_vertex_transform(self._ctx, None, 0, None))
+            return
+        m = (C.c_float * 16)(*[float(x) for x in torch.as_tensor(mvp, dtype=torch.float32).reshape(-1).tolist()])
+        self._model = model
+        self._check(self._lib.cr_set_vertex_transform(self._ctx, model.data_ptr(), model.stride(0), m))
+
     def setIndexBuffer(self, buf, ofs: int, numTris: int) -> None:
         self._need_init()
         ptr = _ptr_of(buf)

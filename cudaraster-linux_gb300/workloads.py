@@ -117,22 +117,28 @@ class FlyThrough:
     """Camera fly-through over an n x n heightfield (2(n-1)^2 triangles) at
     width x height, depth LESS, followed every frame by a translucent water
     layer with about `overlay_frac` of the terrain's triangle count drawn
-    src-over on the same surfaces. Each frame runs the vertex stage on the
-    GPU (cr_vertex_shader_passthrough) into one of three vertex buffers, then
-    the opaque draw (with a deferred clear) and the overlay draw into one of
-    two colour/depth surface pairs."""
+    src-over on the same surfaces. Each frame transforms the vertices -- fused
+    into the setup stage (cr_set_vertex_transform: clip positions computed
+    from the model positions and the frame's MVP, the colour varyings read
+    from one static record buffer per layer), or with fused=False by the
+    separate vertex stage (cr_vertex_shader_passthrough) into one of three
+    record buffers -- then runs the opaque draw (with a deferred clear) and
+    the overlay draw into one of two colour/depth surface pairs. Both give the
+    same bits."""
 
     VERTEX_SLOTS = 3
     TARGETS = 2
 
     def __init__(self, n: int = 4096, width: int = 3840, height: int = 2160, frames: int = 300, seed: int = 5,
-                 overlay_frac: float = 0.1, water_level: float = -0.02, water_alpha: float = 0.35):
+                 overlay_frac: float = 0.1, water_level: float = -0.02, water_alpha: float = 0.35,
+                 fused: bool = True):
         import math
         p = _pkg()
         scenes = importlib.import_module(PKG + ".scenes")
         self.raster = importlib.import_module(PKG + ".raster")
         self.scenes = scenes
         self.n, self.width, self.height, self.frames = n, width, height, frames
+        self.fused = fused
         pos, rgba, tris = scenes.grid_mesh(n, seed)
         m = max(2, int(round((n - 1) * math.sqrt(overlay_frac))) + 1)
         wpos, wrgba, wtris = scenes.water_mesh(m, water_level, water_alpha)
@@ -146,8 +152,16 @@ class FlyThrough:
                 "indices": torch.from_numpy(np.ascontiguousarray(tt, dtype=np.int32)).to(dev),
                 "num_tris": int(tt.shape[0]),
                 "vbuf": [torch.empty((pp.shape[0], 8), dtype=torch.float32, device=dev)
-                         for _ in range(self.VERTEX_SLOTS)],
+                         for _ in range(1 if fused else self.VERTEX_SLOTS)],
             })
+            if fused:   # static records: clip positions come from setup, colours stay
+                vb = self.layers[-1]["vbuf"][0]
+                vb[:, 0:4] = 0.0
+                vb[:, 4:8] = self.layers[-1]["colors"]
+                # Positions padded to 16 bytes: setup gathers each with one vector load.
+                m4 = torch.ones((pp.shape[0], 4), dtype=torch.float32, device=dev)
+                m4[:, 0:3] = self.layers[-1]["model"]
+                self.layers[-1]["model4"] = m4
         self.targets = [(p.CudaSurface((width, height), p.CudaSurface.FORMAT_RGBA8, 1),
                          p.CudaSurface((width, height), p.CudaSurface.FORMAT_DEPTH32, 1)) for _ in range(self.TARGETS)]
         self.mvps = [scenes.terrain_camera(f, width, height).astype(np.float32) for f in range(frames)]
@@ -172,6 +186,8 @@ class FlyThrough:
         return out
 
     def transform(self, frame: int, stream=None) -> None:
+        if self.fused:
+            return   # setup transforms the vertices of each draw (draw_layer)
         slot = frame % self.VERTEX_SLOTS
         for layer in self.layers:
             self.raster.vertex_shader_passthrough(layer["model"], self.mvps[frame], layer["colors"],
@@ -182,7 +198,12 @@ class FlyThrough:
         water) from the frame's vertex slot into its surface pair."""
         color, depth = self.target(frame)
         cr.setSurfaces(color, depth)
-        cr.setVertexBuffer(self.layers[k]["vbuf"][frame % self.VERTEX_SLOTS], 0)
+        layer = self.layers[k]
+        if self.fused:
+            cr.setVertexBuffer(layer["vbuf"][0], 0)
+            cr.setVertexTransform(layer["model4"], self.mvps[frame])
+        else:
+            cr.setVertexBuffer(layer["vbuf"][frame % self.VERTEX_SLOTS], 0)
         if k == 0:
             cr.deferredClear(WATER_CLEAR[:4], WATER_CLEAR[4])
         if sync:
@@ -383,15 +404,16 @@ def run_flythrough_predicted(ft: FlyThrough, frames: int, train_frames: int = 50
 
 FLYTHROUGH_WORKLOAD = ("fly-through: 4096^2 heightfield (33.5M triangles, 6-octave value noise) + translucent water "
                        "layer (10% of the triangles, src-over) at 3840x2160, depth LESS, 300-frame camera loop; "
-                       "per frame the GPU vertex stage and two draws; frames 0-49 plain and training the predictor")
+                       "per frame two draws with the vertex transform fused into setup; frames 0-49 plain and "
+                       "training the predictor")
 
 
 def measure_flythrough(n: int = 4096, width: int = 3840, height: int = 2160, frames: int = 300,
-                       train_frames: int = 50, tuning: dict | None = None, keep: tuple = ()):
+                       train_frames: int = 50, tuning: dict | None = None, keep: tuple = (), fused: bool = True):
     """Plain vs predictor-sized pipelined fly-through over the same frames.
     Returns (summary dict, {frame: (colour, depth)} of the plain pass, the
     FlyThrough)."""
-    ft = FlyThrough(n=n, width=width, height=height, frames=frames)
+    ft = FlyThrough(n=n, width=width, height=height, frames=frames, fused=fused)
     run_flythrough_plain(ft, range(3), tuning)                                   # warm-up
     _, sums, kept, ctr = run_flythrough_plain(ft, range(frames), tuning, checksums=True, keep=keep)
     exact = run_flythrough_predicted(ft, frames, train_frames, tuning, checksums=True)
@@ -435,7 +457,8 @@ def measure_flythrough(n: int = 4096, width: int = 3840, height: int = 2160, fra
                "bit_exact_vs_plain": exact["checksums"] == sums, "frames_checked": len(sums),
                "misses": res["misses"], "miss_rate": round(sum(res["misses"]) / (2 * n_pred), 4),
                "adam_steps": res["adam_steps"], "layers": layers,
-               "plain": "vertex stage + two synchronous drawTriangles per frame",
+               "plain": ("two synchronous drawTriangles per frame, vertex transform fused into setup" if fused
+                         else "vertex stage + two synchronous drawTriangles per frame"),
                "predicted": "queues sized by the predictor two frames ahead, draws queued asynchronously, "
                             "one judge per frame, misses redrawn by the plain path"}
     return summary, kept, ft

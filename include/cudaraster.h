@@ -154,6 +154,16 @@ cr_status cr_deferred_clear(cr_context* ctx, float r, float g, float b, float a,
 cr_status cr_deferred_clear_raw(cr_context* ctx, uint32_t abgr, uint32_t encoded_depth);
 cr_status cr_set_pixel_pipe(cr_context* ctx, const char* name);
 cr_status cr_set_vertex_buffer(cr_context* ctx, const void* vertices, int64_t offset_bytes);
+/* Fused vertex transform (no counterpart in the reference): while set, the
+ * setup stage of cr_draw_triangles / _async takes each vertex's clip position
+ * as mvp * (model[i].xyz, 1) -- vertexShader_passthrough (test/shader/
+ * PassThrough.cu:16-35) with the same operation order, so the output bits are
+ * those of running that shader first -- instead of reading the vertex
+ * record's clipPos; the records still supply the varyings. model: device
+ * array, model_stride floats per vertex (>= 3); mvp: 16 row-major floats,
+ * copied. model NULL turns it off. Batched and static draws ignore it. */
+cr_status cr_set_vertex_transform(cr_context* ctx, const float* model, int32_t model_stride,
+                                  const float* mvp_row_major);
 cr_status cr_set_index_buffer(cr_context* ctx, const void* indices, int64_t offset_bytes,
                               int32_t num_tris);
 cr_status cr_set_tuning(cr_context* ctx, const cr_tuning* tuning);

@@ -102,6 +102,13 @@ struct DrawDev {
     S32 unitEntries;          // bin entries per coarse unit; <= 0: sized on the device from the bin entries
     S32 unitTarget;           // coarse units wanted when sized on the device (set by the launcher)
     S64 totalTris;
+    // Fused vertex transform (single draws): when model is set, setup takes a
+    // vertex's clip position as mvp * (model[i], 1) -- the reference's
+    // vertexShader_passthrough -- instead of reading the record's clipPos.
+    const float* model;       // xyz at modelStride floats per vertex, or null
+    S32 modelStride;
+    S32 modelVec4;            // stride 4 and 16-byte aligned: one vector load per vertex
+    F32 mvp[16];              // row-major
     // setup
     uint8_t* triSubtris;      // [totalTris]
     uint4* triHeader;         // [maxSubtris]

@@ -173,6 +173,42 @@ __device__ __noinline__ void setupClipped(const DrawDev& d, S64 gt, int3 vidx, f
 }
 
 // Resident setup CTAs per SM the compiler must allow (register budget).
+// Clip position of vertex i: its record's clipPos, or, with the fused vertex
+// transform, mvp * (model[i], 1) with each row summed left to right from zero
+// as vertexShader_passthrough (PassThrough.cu:16-35, Math.hpp:990-1001)
+// writes it, so both give the same bits. d.mvp lives in the kernel's
+// parameter space.
+__device__ __forceinline__ float4 transformModel(const DrawDev& d, int i) {
+    const float* p = d.model + (S64)i * d.modelStride;
+    F32 x, y, z;
+    if (d.modelVec4) {
+        const float4 q = __ldg((const float4*)p);
+        x = q.x, y = q.y, z = q.z;
+    } else {
+        x = __ldg(p + 0), y = __ldg(p + 1), z = __ldg(p + 2);
+    }
+    F32 r[4];
+#pragma unroll
+    for (int row = 0; row < 4; row++)
+        r[row] = fadd(fadd(fadd(fadd(0.0f, fmul(d.mvp[row * 4 + 0], x)), fmul(d.mvp[row * 4 + 1], y)),
+                           fmul(d.mvp[row * 4 + 2], z)),
+                      fmul(d.mvp[row * 4 + 3], 1.0f));
+    return make_float4(r[0], r[1], r[2], r[3]);
+}
+
+__device__ __forceinline__ void fetchClip(const DrawDev& d, const float4* verts, S32 stride4, int3 vidx, float4& v0,
+                                          float4& v1, float4& v2) {
+    if (d.model == nullptr) {
+        v0 = __ldg(&verts[(S64)vidx.x * stride4]);
+        v1 = __ldg(&verts[(S64)vidx.y * stride4]);
+        v2 = __ldg(&verts[(S64)vidx.z * stride4]);
+    } else {
+        v0 = transformModel(d, vidx.x);
+        v1 = transformModel(d, vidx.y);
+        v2 = transformModel(d, vidx.z);
+    }
+}
+
 #ifndef CR_SETUP_MIN_BLOCKS
 #define CR_SETUP_MIN_BLOCKS 5
 #endif
@@ -191,9 +227,8 @@ __global__ void __launch_bounds__(256, CR_SETUP_MIN_BLOCKS) setupKernel(DrawDev 
     S64 t = gt - __ldg(&in->triBase);
 
     int3 vidx = make_int3(__ldg(&indices[3 * t + 0]), __ldg(&indices[3 * t + 1]), __ldg(&indices[3 * t + 2]));
-    float4 v0 = __ldg(&verts[(S64)vidx.x * stride4]);
-    float4 v1 = __ldg(&verts[(S64)vidx.y * stride4]);
-    float4 v2 = __ldg(&verts[(S64)vidx.z * stride4]);
+    float4 v0, v1, v2;
+    fetchClip(d, verts, stride4, vidx, v0, v1, v2);
 
     // Outside view frustum => cull (TriangleSetup.inl:262-281).
     if ((v0.w < fabsf(v0.x)) | (v0.w < fabsf(v0.y)) | (v0.w < fabsf(v0.z))) {
