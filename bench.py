@@ -222,6 +222,29 @@ def flythrough_oracle_check(ft, kept, f):
             "oracle_s": round(time.perf_counter() - t0, 1)}
 
 
+def textured_oracle_check(tex):
+    """The textured frame against the CPU oracle: the GPU's shaded vertices against the
+    vertex oracle, then the frame (all host cores)."""
+    import time
+    from oracle import oracle as orc
+    from oracle import vertex_oracle
+    pkg = importlib.import_module(PKG)
+    workloads = importlib.import_module(PKG + ".workloads")
+    _, (color, depth), sc, shaded = tex
+    t0 = time.perf_counter()
+    k = (sc["pos_to_clip"], sc["pos_to_camera"], sc["normal_to_camera"])
+    verts = vertex_oracle.vertex_tex_phong(sc["input"], *k)
+    vertex_exact = bool(np.array_equal(verts.view(np.uint32), shaded.cpu().numpy().view(np.uint32)))
+    orc.set_tex_phong(sc["materials"], sc["triangle_material_idx"], sc["atlas"])
+    clear = (pkg.color_to_abgr(*workloads.CLEAR[:4]), pkg.clear_depth_from_float(workloads.CLEAR[4]))
+    p = orc.make_pipe(sc["width"], sc["height"], 1, orc.DEPTH | orc.LERP, "replace", "texphong", 64, clear)
+    rc, rd, st = orc.render(p, verts, sc["indices"], None, None, 0)
+    gc = color.cpu().numpy().view(np.uint32)
+    gd = depth.cpu().numpy().view(np.uint32)
+    return {"vertices_bit_exact": vertex_exact, "bit_exact": bool((gc == rc).all() and (gd == rd).all()),
+            "zmin_violations": int(st["zmin_violations"]), "oracle_s": round(time.perf_counter() - t0, 1)}
+
+
 def subpixel_oracle_check(sc, got):
     """The 4x MSAA heightfield frame against the CPU oracle (all host cores)."""
     import time
@@ -248,6 +271,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the uneven-batch comparison")
     ap.add_argument("--no-flythrough", action="store_true", help="skip the fly-through with the queue predictor")
     ap.add_argument("--no-subpixel", action="store_true", help="skip the 4x MSAA grazing-heightfield frame")
+    ap.add_argument("--no-textured", action="store_true",
+                    help="skip the textured Phong frame and the vertex-shader throughput lines")
     ap.add_argument("--profile-frames", type=int, default=0,
                     help="only draw this many frames of the workload (for ncu captures), print nothing else")
     ap.add_argument("--profile-workload", default="soup1m", choices=["soup1m", "subpixel", "flythrough", "flythrough2048",
@@ -439,6 +464,11 @@ def main():
     if rank == 0 and not args.no_subpixel:
         sub = workloads.measure_subpixel(tuning=workloads.load_tuning("subpixel"))
         line["subpixel_stress"] = sub[0]
+    tex = None
+    if rank == 0 and not args.no_textured:
+        tex = workloads.measure_textured(tuning=workloads.load_tuning("subpixel"))
+        line["textured"] = tex[0]
+        line["vertex_shaders"] = workloads.measure_vertex_shaders(peak_gbs=peaks()[0])
     fly = None
     if rank == 0 and not args.no_flythrough:
         fly = workloads.measure_flythrough(tuning=workloads.load_tuning("flythrough"), keep=(FLY_ORACLE_FRAME,))
@@ -453,6 +483,8 @@ def main():
             line["flythrough"]["oracle_frame"] = flythrough_oracle_check(fly[2], fly[1], FLY_ORACLE_FRAME)
         if sub is not None:
             line["subpixel_stress"]["oracle"] = subpixel_oracle_check(sub[2], sub[1])
+        if tex is not None:
+            line["textured"]["oracle"] = textured_oracle_check(tex)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -548,3 +548,108 @@ def profile_frames(name: str, frames: int, tuning: dict | None = None) -> dict:
         res = run_flythrough_predicted(ft, frames, max(3, (2 * frames) // 3), tuning)
         return {"profile": name, "frames": frames, "misses": res["misses"], "adam_steps": res["adam_steps"]}
     raise ValueError(name)
+
+
+TEXTURED_WORKLOAD = ("textured Phong: 2048^2 heightfield (8.4M triangles) as InputVertex records, four materials "
+                     "(untextured, diffuse texture, diffuse + alpha-tested texture, second texture) from one "
+                     "mip-mapped RGBA8 atlas, 3840x2160, 1 spp, depth LESS; per frame vertexShader_texPhong on the "
+                     "GPU and one PixelPipe_texPhong draw; L2 flushed before each frame")
+
+
+def measure_textured(n: int = 2048, width: int = 3840, height: int = 2160, frame: float = 120.0, steps: int = 10,
+                     warmup: int = 3, tuning: dict | None = None):
+    """The textured Phong pipe per frame: the texPhong vertex shader then one draw.
+    Returns (summary, (colour, depth) tensors of the last frame, scene, shaded vertices)."""
+    p = _pkg()
+    scenes = importlib.import_module(PKG + ".scenes")
+    raster = importlib.import_module(PKG + ".raster")
+    sc = scenes.textured_terrain(n, width, height, seed=5, frame=frame)
+    T = int(sc["indices"].shape[0])
+    cr = p.CudaRaster()
+    cr.init()
+    if tuning:
+        cr.setTuning(**tuning)
+    color = p.CudaSurface((width, height), p.CudaSurface.FORMAT_RGBA8, 1)
+    depth = p.CudaSurface((width, height), p.CudaSurface.FORMAT_DEPTH32, 1)
+    cr.setSurfaces(color, depth)
+    cr.setPixelPipe(None, "PixelPipe_texPhong")
+    inp = torch.from_numpy(sc["input"]).cuda()
+    shaded = torch.empty((inp.shape[0], 16), dtype=torch.float32, device="cuda")
+    mats = torch.from_numpy(sc["materials"]).cuda()
+    tri = torch.from_numpy(sc["triangle_material_idx"]).cuda()
+    atlas = torch.from_numpy(sc["atlas"].view(np.int32)).cuda()
+    raster.set_tex_phong_constants(mats, tri, atlas)
+    i = torch.from_numpy(np.ascontiguousarray(sc["indices"], dtype=np.int32)).cuda()
+    cr.setVertexBuffer(shaded, 0)
+    cr.setIndexBuffer(i, 0, T)
+    k = (sc["pos_to_clip"], sc["pos_to_camera"], sc["normal_to_camera"])
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def frame_fn():
+        raster.vertex_shader_tex_phong(inp, *k, out=shaded, stream=stream)
+        cr.deferredClear(CLEAR[:4], CLEAR[4])
+        cr.drawTriangles(stream)
+
+    for _ in range(warmup):
+        frame_fn()
+    ms, stages = [], []
+    for _ in range(steps):
+        flush.fill_(1)
+        ms += time_events(frame_fn, 1, stream)
+        st = cr.getStats()
+        stages.append([st.setupTime, st.binTime, st.coarseTime, st.fineTime])
+    c = cr.getCounters()
+    med = float(np.median(ms))
+    st_ms = np.median(np.array(stages), axis=0) * 1e3
+    summary = {"workload": TEXTURED_WORKLOAD, "num_tris": T, "num_vertices": int(inp.shape[0]), "width": width,
+               "height": height, "frames_per_s": round(1000.0 / med, 2), "ms_per_frame": round(med, 4),
+               "mtri_per_s": round(T / med / 1e3, 1),
+               "stage_ms": {"setup": round(st_ms[0], 4), "bin": round(st_ms[1], 4), "coarse": round(st_ms[2], 4),
+                            "fine": round(st_ms[3], 4)},
+               "counters": {key: c[key] for key in ("num_subtris", "bin_entries", "tile_entries", "reruns",
+                                                    "overflow")}}
+    return summary, (color.tensor, depth.tensor), sc, shaded
+
+
+def measure_vertex_shaders(n: int = 4096 * 4096, steps: int = 10, warmup: int = 3, peak_gbs: float | None = None):
+    """The vertex shaders over n vertices (inputs far larger than L2, so no flush is
+    needed): median time per launch, vertices/s and algorithmic bytes per second --
+    passthrough 12 B position + 16 B colour in, 32 B out; Gouraud 32 B InputVertex +
+    4 B material index in, 32 B out (the material table stays cached); texPhong 32 B
+    in, 64 B out."""
+    raster = importlib.import_module(PKG + ".raster")
+    scenes = importlib.import_module(PKG + ".scenes")
+    g = torch.Generator(device="cuda").manual_seed(3)
+    inp = torch.rand((n, 8), generator=g, device="cuda", dtype=torch.float32) * 2.0 - 1.0
+    model = inp[:, 0:3].contiguous()
+    colors = torch.rand((n, 4), generator=g, device="cuda", dtype=torch.float32)
+    midx = torch.randint(0, 4, (n,), generator=g, device="cuda", dtype=torch.int32)
+    mats = torch.from_numpy(raster.material_records([[0.7, 0.6, 0.5, 1.0]] * 4, [[0.3, 0.3, 0.3]] * 4,
+                                                    [8.0, 16.0, 32.0, 64.0])).cuda()
+    view = scenes.look_at((1.5, 2.0, 3.0), (0.0, 0.0, 0.0)).astype(np.float32)
+    clip = (scenes.perspective(60.0, 16 / 9, 0.1, 100.0) @ view).astype(np.float32)
+    normal = view[:3, :3].copy()
+    out8 = torch.empty((n, 8), dtype=torch.float32, device="cuda")
+    out16 = torch.empty((n, 16), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    shaders = {
+        "passthrough": (lambda: raster.vertex_shader_passthrough(model, clip, colors, out=out8, stream=stream),
+                        12 + 16 + 32),
+        "gouraud": (lambda: raster.vertex_shader_gouraud(inp, clip, view, normal, mats, midx, out=out8,
+                                                         stream=stream), 32 + 4 + 32),
+        "tex_phong": (lambda: raster.vertex_shader_tex_phong(inp, clip, view, normal, out=out16, stream=stream),
+                      32 + 64),
+    }
+    res = {}
+    for name, (fn, per_vertex) in shaders.items():
+        for _ in range(warmup):
+            fn()
+        med = float(np.median(time_events(fn, steps, stream)))
+        gbs = n * per_vertex / (med * 1e-3) / 1e9
+        res[name] = {"ms": round(med, 4), "gvertices_per_s": round(n / med / 1e6, 2),
+                     "alg_bytes_per_vertex": per_vertex, "achieved_gbs": round(gbs, 1)}
+        if peak_gbs:
+            res[name]["frac_of_measured_hbm"] = round(gbs / peak_gbs, 4)
+    return {"workload": f"{n:,} vertices (random InputVertex records), each shader timed alone", "vertices": n,
+            "shaders": res}
