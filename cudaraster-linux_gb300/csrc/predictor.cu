@@ -14,7 +14,7 @@
  *
  * The reference has no counterpart: it sizes its queues on the host from the
  * previous draw and grows them when a draw overflows (CudaRaster.cpp:263-275,
- * 325-342). That grow-and-rerun path stays the fallback and the judge of
+ * 325-342). That grow-and-rerun path stays the fallback and the check of
  * every prediction; a prediction can cost a rerun, never an output bit.
  */
 #include <cuda_runtime.h>

@@ -8,7 +8,7 @@ pair (previous frame's histogram + camera delta -> this frame's occupancy),
 and predicts the next frame's bin- and tile-queue occupancy, from which the
 queue capacities of the next draw are set (CudaRaster.setCapacity). A draw
 whose queues overflow anyway is redrawn by the plain overflow-detect-and-
-rerun path, which also judges the predictor's misses.
+rerun path, which also catches and redraws the predictor's misses.
 
 The reference has no learned part: it sizes its queues from the previous
 draw and grows them on overflow (src/cudaraster/CudaRaster.cpp:263-275,
@@ -204,7 +204,7 @@ class QueuePredictor:
     correct the extrapolated trend of the bin- and tile-entry totals (an
     untrained network, whose output layer starts at zero, predicts that
     trend). ahead = 2 lets a host keep one frame queued while the previous one
-    is judged.
+    is checked.
 
     Per frame, after the draw and in stream order: ``step(raster, k,
     camera_delta_ahead)`` -- one fused launch (cr_predictor_frame) that turns
@@ -213,7 +213,7 @@ class QueuePredictor:
     host. After a sync the host reads ``predicted_totals(k + ahead)`` and
     ``counters_of(k)``, and sizes that draw with ``capacity()``. ``train``
     takes Adam steps on random mini-batches of the samples whose target
-    frames have been judged. Sample k pairs frame k's input (pooled
+    frames have been checked. Sample k pairs frame k's input (pooled
     histogram and camera move, x_pool[k % pool]) with the change to frame
     k + ahead (t_pool[k % pool]).
     """
@@ -265,10 +265,10 @@ class QueuePredictor:
             self.fetch_host[k % R].copy_(self.fetch_dev[k % R], non_blocking=True)
         self.stepped = max(self.stepped, k)
 
-    def train(self, steps: int, judged_upto: int, stream=None):
+    def train(self, steps: int, checked_upto: int, stream=None):
         """Adam steps on random mini-batches of the samples whose target frame
-        is at most `judged_upto` and whose input is still in the pool."""
-        newest = judged_upto - self.ahead
+        is at most `checked_upto` and whose input is still in the pool."""
+        newest = checked_upto - self.ahead
         oldest = max(0, self.stepped - self.pool + 1)
         avail = newest - oldest + 1
         if avail <= 0:

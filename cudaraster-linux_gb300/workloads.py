@@ -271,7 +271,7 @@ def run_flythrough_predicted(ft: FlyThrough, frames: int, train_frames: int = 50
     """The first `train_frames` frames are plain (synchronous draws) and train
     one predictor per layer on the counts they emit. Later frames are drawn
     asynchronously into queues sized from predictions made `ahead` (= 2)
-    frames earlier, so the host keeps one frame queued: at frame f it judges
+    frames earlier, so the host keeps one frame queued: at frame f it checks
     frame f - 2 (its overflow flags), then sizes and launches frame f. Each
     layer's predictor step runs on its own stream right after that layer's
     draw, and the next draw of the layer waits for it. A frame whose queues
@@ -319,7 +319,7 @@ def run_flythrough_predicted(ft: FlyThrough, frames: int, train_frames: int = 50
         if f in keep:
             kept[f] = ft.snapshot(f)
 
-    def judge(f):
+    def check_frame(f):
         """Frame f's steps have completed; redraw it if a queue overflowed."""
         ctr = [pr.counters_of(f) for pr in preds]
         missed = [int(c[5]) != 0 for c in ctr]
@@ -370,13 +370,13 @@ def run_flythrough_predicted(ft: FlyThrough, frames: int, train_frames: int = 50
 
     t0 = time.perf_counter()
     for f in range(train_frames, frames + ahead):
-        j = f - ahead                    # the frame to judge now
+        j = f - ahead                    # the frame to check now
         tw = time.perf_counter()
         for k in range(L):
             ev_pred[k][j % R].synchronize()
         wait += time.perf_counter() - tw
         if j >= train_frames:
-            judge(j)
+            check_frame(j)
         if f >= frames:
             continue
         caps = []
@@ -460,7 +460,7 @@ def measure_flythrough(n: int = 4096, width: int = 3840, height: int = 2160, fra
                "plain": ("two synchronous drawTriangles per frame, vertex transform fused into setup" if fused
                          else "vertex stage + two synchronous drawTriangles per frame"),
                "predicted": "queues sized by the predictor two frames ahead, draws queued asynchronously, "
-                            "one judge per frame, misses redrawn by the plain path"}
+                            "one overflow check per frame, misses redrawn by the plain path"}
     return summary, kept, ft
 
 

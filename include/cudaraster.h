@@ -327,7 +327,7 @@ cr_status cr_resolve_color(const void* color, int32_t width, int32_t height, int
 /* ---- Queue occupancy and the learned queue predictor ----
  * No reference counterpart: the reference sizes its queues from the previous
  * draw and grows them on overflow (CudaRaster.cpp:263-275, 325-342), which
- * stays the fallback and the judge of every prediction made here. */
+ * stays the fallback and the check of every prediction made here. */
 
 /* Bin and tile grid of the last draw (of its first instance for a batch). */
 typedef struct cr_queue_layout {

@@ -229,7 +229,7 @@ public:
         needInit();
         crdetail::check(cr_draw_triangles(m_ctx, m_stream), m_ctx);
     }
-    // No read-back: the caller judges the counters later (cr_get_counters).
+    // No read-back: the caller reads the counters later (cr_get_counters).
     void drawTrianglesAsync() {
         needInit();
         crdetail::check(cr_draw_triangles_async(m_ctx, m_stream), m_ctx);
