@@ -91,3 +91,27 @@ def test_lit_mesh_renders_as_oracle(cuda):
     rc, rd, st = oracle_render("PixelPipe_gouraud", sc, clear)
     assert st["zmin_violations"] == 0
     assert_same(gc, gd, rc, rd, "lit heightfield")
+
+
+def test_vertex_shaders_unaligned_records(cuda):
+    # texPhong records only 4-byte aligned take the per-thread path, 16-byte aligned
+    # ones are staged through shared memory; both give the oracle's bits, also for a
+    # vertex count that leaves the last block partly empty (Gouraud takes the
+    # per-thread path either way).
+    raster = pkg_mod("raster")
+    clip, view, normal = _camera()
+    v, mats, idx = _inputs(10_007, 8)
+    flat = torch.zeros(v.size + 1, dtype=torch.float32, device="cuda")
+    flat[1:] = torch.from_numpy(v.reshape(-1)).cuda()
+    shifted = flat[1:].view(v.shape)
+    assert shifted.data_ptr() % 16 == 4
+    aligned = torch.from_numpy(v).cuda()
+    m = torch.from_numpy(mats).cuda()
+    i = torch.from_numpy(idx).cuda()
+    ref_g = vo.vertex_gouraud(v, clip, view, normal, mats, idx).view(np.uint32)
+    ref_t = vo.vertex_tex_phong(v, clip, view, normal).view(np.uint32)
+    for src in (shifted, aligned):
+        g = raster.vertex_shader_gouraud(src, clip, view, normal, m, i).cpu().numpy()
+        t = raster.vertex_shader_tex_phong(src, clip, view, normal).cpu().numpy()
+        assert np.array_equal(g.view(np.uint32), ref_g)
+        assert np.array_equal(t.view(np.uint32), ref_t)
