@@ -115,3 +115,36 @@ def test_overflow_rerun_is_exact(cuda):
     c, d, cnt, _ = gpu_render("PixelPipe_gouraud", sc, clear, capacity=(20001, 1000, 1000))
     assert cnt["reruns"] >= 1 and cnt["overflow"] == 0
     assert_same(c, d, base_c, base_d, "overflow rerun")
+
+
+def test_batch_with_textured_pipes(cuda):
+    # Textured Phong instances (1 and 4 samples, one constant set) batched with
+    # Gouraud soups: each framebuffer equals its single draw, bit for bit.
+    raster = pkg_mod("raster")
+    scenes = pkg_mod("scenes")
+    tsc = scenes.textured_terrain(64, 320, 240, seed=12)
+    k = [tsc["pos_to_clip"], tsc["pos_to_camera"], tsc["normal_to_camera"]]
+    shaded = raster.vertex_shader_tex_phong(torch.from_numpy(tsc["input"]).cuda(), *k).cpu().numpy()
+    mats = torch.from_numpy(tsc["materials"]).cuda()
+    tri = torch.from_numpy(tsc["triangle_material_idx"]).cuda()
+    atlas = torch.from_numpy(tsc["atlas"].view(np.int32)).cuda()
+    raster.set_tex_phong_constants(mats, tri, atlas)
+    textured = {"vertices": shaded, "indices": tsc["indices"], "width": 320, "height": 240}
+    textured4 = dict(textured, width=200, height=150)
+    items = [("PixelPipe_gouraud", pkg_mod("scenes").soup(4000, 256, 192, seed=31, median_px=5.0)),
+             ("PixelPipe_texPhong", textured),
+             ("PixelPipe_texPhong_msaa4", textured4),
+             ("PixelPipe_gouraud_srcover", pkg_mod("scenes").soup(2500, 300, 220, seed=32, median_px=5.0,
+                                                                   alpha_range=(0.2, 1.0)))]
+    p = pkg()
+    cr = p.CudaRaster()
+    cr.init()
+    insts, keep = _instances(items, (0.1, 0.2, 0.3, 1.0, 1.0))
+    cr.drawBatch(insts)
+    torch.cuda.synchronize()
+    for (pipe, sc), (cs, ds, _, _) in zip(items, keep):
+        gc = cs.download().numpy().astype(np.uint32)
+        gd = ds.download().numpy().astype(np.uint32)
+        rc, rd, _, _ = gpu_render(pipe, sc, _clear())
+        assert_same(gc, gd, rc, rd, f"batched {pipe}")
+        assert (rc != _clear()[0]).any()
