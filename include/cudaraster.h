@@ -5,6 +5,11 @@
  * noted) and returns a cr_status. The C++ drop-in classes in
  * include/cudaraster/CudaRaster.hpp are a header-only layer over this file.
  *
+ * Threading: a cr_context is not thread-safe -- one host thread at a time
+ * per context, as with the reference's CudaRaster; separate contexts may be
+ * used from separate threads. Work is ordered on the stream each call takes
+ * (NULL: the legacy default stream).
+ *
  * Reference interface replaced (tcoppex/cudaraster-linux):
  *   CudaRaster::init                 src/cudaraster/CudaRaster.cpp:98-128      -> cr_create
  *   CudaRaster::~CudaRaster          src/cudaraster/CudaRaster.cpp:80-94       -> cr_destroy
