@@ -521,7 +521,15 @@ def profile_frames(name: str, frames: int, tuning: dict | None = None) -> dict:
     (plain fly-through frames 100..100+frames over the 4096^2 or a 2048^2
     heightfield), "predicted" (a short predictor-sized fly-through: `frames`
     frames, the first two thirds plain and training) or "batch64" (`frames`
-    replays of the uneven 64-scene batch's CUDA graph)."""
+    replays of the uneven 64-scene batch's CUDA graph), "textured" (frames of
+    the textured Phong heightfield: its vertex shader and one draw each) or
+    "vertex" (`frames` launches of each vertex shader over 8M vertices)."""
+    if name == "textured":
+        s, _, _, _ = measure_textured(steps=frames, warmup=0, tuning=tuning)
+        return {"profile": name, "frames": frames, "counters": s["counters"]}
+    if name == "vertex":
+        v = measure_vertex_shaders(n=8 << 20, steps=frames, warmup=0)   # 268 MB of input records, above L2
+        return {"profile": name, "frames": frames, "vertices": v["vertices"]}
     if name == "batch64":
         p = _pkg()
         scenes = importlib.import_module(PKG + ".scenes")
