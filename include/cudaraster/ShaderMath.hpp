@@ -152,6 +152,20 @@ __device__ __forceinline__ void crTexAxis(F32 u, S32 n, S32& i0, S32& i1, U32& w
     i1 = i0 + 1 == n ? 0 : i0 + 1;
 }
 
+// s / (255 * 65536), correctly rounded, for integers 0 <= s <= 255 * 65536:
+// RN(s / 255) by one multiplication by RN(1 / 255) and one FMA-based
+// correction (Markstein), then the exact scaling by 2^-16. Equal to the IEEE
+// division for every s in the range -- checked exhaustively on the CPU with
+// IEEE fmaf -- at three instructions instead of a division.
+__device__ __forceinline__ F32 crTexNormalize(U32 s) {
+    const F32 x = (F32)s;  // < 2^24: exact
+    const F32 rcp = 0.00392156886f;  // RN(1 / 255)
+    const F32 q0 = __fmul_rn(x, rcp);
+    const F32 r = __fmaf_rn(-q0, 255.0f, x);
+    const F32 q = __fmaf_rn(r, rcp, q0);
+    return __fmul_rn(q, 1.52587890625e-05f);  // 2^-16
+}
+
 // tex2D of an atlas with linear filtering, wrap addressing and normalized
 // coordinates, returning channels in [0, 1].
 __device__ __forceinline__ Vec4f crTex2D(const TextureAtlas& t, F32 u, F32 v) {
@@ -169,7 +183,7 @@ __device__ __forceinline__ Vec4f crTex2D(const TextureAtlas& t, F32 u, F32 v) {
         const int sh = 8 * k;
         const U32 s = w00 * ((c00 >> sh) & 255u) + w10 * ((c10 >> sh) & 255u) + w01 * ((c01 >> sh) & 255u) +
                       w11 * ((c11 >> sh) & 255u);  // < 2^24: exact as a float
-        out[k] = __fdiv_rn((F32)s, 16711680.0f);  // 255 * 65536
+        out[k] = crTexNormalize(s);  // s / (255 * 65536)
     }
     return Vec4f(out[0], out[1], out[2], out[3]);
 }

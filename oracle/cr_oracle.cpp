@@ -1086,6 +1086,22 @@ void or_texture_sample(const uint32_t* atlas, int atlas_width, int atlas_height,
     for (int64_t i = 0; i < n; i++) tex2d(atlas, atlas_width, atlas_height, uv[2 * i], uv[2 * i + 1], out + 4 * i);
 }
 
+// The GPU filter's division-free form of s / (255 * 65536) (ShaderMath.hpp
+// crTexNormalize) against the division the specification states, for every
+// weighted sum s the filter can form; returns the number of differences.
+int64_t or_tex_normalize_mismatches(void) {
+    const F32 rcp = 0.00392156886f;
+    int64_t bad = 0;
+    for (U32 s = 0; s <= 16711680u; s++) {
+        const F32 x = (F32)s;
+        const F32 q0 = x * rcp;
+        const F32 r = std::fmaf(-q0, 255.0f, x);
+        const F32 q = std::fmaf(r, rcp, q0);
+        if (q * 1.52587890625e-05f != x / 16711680.0f) bad++;
+    }
+    return bad;
+}
+
 float or_pow_exact(float x, float y) { return pow_exact(x, y); }
 float or_log2_exact(float x) { return log2_full(x); }
 

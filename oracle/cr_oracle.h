@@ -121,6 +121,9 @@ void     or_set_tex_phong(const float* materials, int num_materials, const int32
 /* The atlas filter (bilinear, wrap, normalized coordinates, 8-bit weights). */
 void     or_texture_sample(const uint32_t* atlas, int atlas_width, int atlas_height, const float* uv,
                            float* out, int64_t n);
+/* Differences between the GPU filter's division-free normalisation and the
+ * specified division, over every weighted sum the filter can form (0 expected). */
+int64_t  or_tex_normalize_mismatches(void);
 /* The exactly specified power / log2 and evaluateLighting (Shaders.cu:37-50). */
 float    or_pow_exact(float x, float y);
 float    or_log2_exact(float x);

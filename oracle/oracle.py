@@ -73,6 +73,7 @@ def load():
             ("or_set_tex_phong", None, [C.c_void_p, C.c_int, C.c_void_p, C.c_int64, C.c_void_p, C.c_int, C.c_int]),
             ("or_texture_sample", None, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int64]),
             ("or_pow_exact", C.c_float, [C.c_float, C.c_float]),
+            ("or_tex_normalize_mismatches", C.c_int64, []),
             ("or_log2_exact", C.c_float, [C.c_float]),
             ("or_evaluate_lighting", None, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p]),
         ]:

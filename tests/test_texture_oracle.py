@@ -93,3 +93,9 @@ def test_cpp_lighting_matches_vertex_oracle():
     for i in range(n):
         c = orc.evaluate_lighting(v[i, 0:3], v[i, 3:6], mats[0, 4:7], mats[0, 7], mats[0, 0:3])
         assert np.array_equal(c.view(np.uint32), out[i, 4:7].view(np.uint32))
+
+
+def test_division_free_normalisation_is_exact():
+    # The GPU filter divides its weighted sums by 255 * 65536 with a multiplication and
+    # two FMAs; over every sum it can form that equals the IEEE division bit for bit.
+    assert orc.load().or_tex_normalize_mismatches() == 0
