@@ -167,7 +167,7 @@ __device__ __forceinline__ F32 fmul(F32 a, F32 b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ F32 fadd(F32 a, F32 b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ F32 fsub(F32 a, F32 b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ F32 fdiv(F32 a, F32 b) { return __fdiv_rn(a, b); }
-__device__ __forceinline__ F32 frcp(F32 a) { return __fdiv_rn(1.0f, a); }
+__device__ __forceinline__ F32 frcp(F32 a) { return __frcp_rn(a); }  // 1 / a, correctly rounded (= __fdiv_rn(1, a))
 __device__ __forceinline__ S32 min3i(S32 a, S32 b, S32 c) { return min(min(a, b), c); }
 __device__ __forceinline__ S32 max3i(S32 a, S32 b, S32 c) { return max(max(a, b), c); }
 // shr.s64 semantics: shift amounts >= 64 give the sign fill.
