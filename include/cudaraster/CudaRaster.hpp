@@ -222,6 +222,15 @@ public:
         needInit();
         crdetail::check(cr_set_index_buffer(m_ctx, buf ? buf->getCudaPtr() : nullptr, ofs, numTris), m_ctx);
     }
+    // Beyond the reference: vertexShader_passthrough fused into setup
+    // (cr_set_vertex_transform). `model` holds xyz at modelStride floats per
+    // vertex; mvpRowMajor is 16 floats; a null model turns it off.
+    void setVertexTransform(Buffer* model, int modelStride, const float* mvpRowMajor) {
+        needInit();
+        crdetail::check(cr_set_vertex_transform(m_ctx, model ? (const float*)model->getCudaPtr() : nullptr,
+                                                modelStride, mvpRowMajor),
+                        m_ctx);
+    }
 
     // CudaRaster.cpp:237-342: draws, reads the overflow counters back and
     // reruns with grown queues until nothing overflowed.
