@@ -826,7 +826,9 @@ __device__ __forceinline__ void fineTiles(const DrawDev& d, int group, S32 tileB
 // The fine-stage kernel. At one sample the register budget is pinned to five
 // resident CTAs per SM (48 registers); with MSAA the compiler's own choice
 // measured faster than any pinned budget (4x MSAA: 63 registers, 0.58 ms on
-// the 4K grid, against 0.60 ms pinned to four CTAs and 0.64 ms to three).
+// the 4K grid, against 0.60 ms pinned to four CTAs, 0.64 ms to three and
+// 0.645 ms to five, where 48 registers fit without spills but with more
+// instructions).
 template <class V, class FS, class BS, int S, U32 F>
 __global__ void __launch_bounds__(kFineMaxThreads, 5) fineKernel1(DrawDev d, int group, S32 tileBegin, S32 tileEnd) {
     fineTiles<V, FS, BS, S, F>(d, group, tileBegin, tileEnd);
