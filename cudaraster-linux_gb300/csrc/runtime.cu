@@ -343,6 +343,22 @@ cr_status cr_set_vertex_buffer(cr_context* ctx, const void* vertices, int64_t of
     return CR_OK;
 }
 
+cr_status cr_read_setup_output(cr_context* ctx, uint8_t* tri_subtris, uint32_t* tri_header, uint32_t* tri_data,
+                               int64_t max_slots, int64_t* num_tris, int64_t* num_slots) {
+    if (!ctx || !num_tris || !num_slots || max_slots < 0) return CR_ERR_INVALID_ARGUMENT;
+    const int64_t t = ctx->last.num_tris, n = ctx->last.num_subtris;
+    *num_tris = t;
+    *num_slots = n;
+    if (ctx->last.overflow) return fail(ctx, CR_ERR_INVALID_STATE, "CudaRaster: the last draw overflowed");
+    if (n > max_slots) return fail(ctx, CR_ERR_CAPACITY, "CudaRaster: %lld setup slots do not fit", (long long)n);
+    if (n == 0) return CR_OK;
+    CR_CUDA(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+    if (tri_subtris) CR_CUDA(cudaMemcpy(tri_subtris, ctx->triSubtris.ptr, (size_t)t, cudaMemcpyDeviceToHost), "cudaMemcpy");
+    if (tri_header) CR_CUDA(cudaMemcpy(tri_header, ctx->triHeader.ptr, (size_t)n * 16, cudaMemcpyDeviceToHost), "cudaMemcpy");
+    if (tri_data) CR_CUDA(cudaMemcpy(tri_data, ctx->triData.ptr, (size_t)n * 64, cudaMemcpyDeviceToHost), "cudaMemcpy");
+    return CR_OK;
+}
+
 cr_status cr_set_vertex_transform(cr_context* ctx, const float* model, int32_t model_stride,
                                   const float* mvp_row_major) {
     if (!ctx) return CR_ERR_INVALID_ARGUMENT;

@@ -159,6 +159,16 @@ cr_status cr_deferred_clear(cr_context* ctx, float r, float g, float b, float a,
 cr_status cr_deferred_clear_raw(cr_context* ctx, uint32_t abgr, uint32_t encoded_depth);
 cr_status cr_set_pixel_pipe(cr_context* ctx, const char* name);
 cr_status cr_set_vertex_buffer(cr_context* ctx, const void* vertices, int64_t offset_bytes);
+/* Inspection of the last single draw's setup output (the intermediate
+ * buffers the reference exposed for its per-stage debugging, CudaRaster.hpp:
+ * 53-67): per triangle its subtriangle count [num_tris], then every slot's
+ * CRTriangleHeader (4 words) and CRTriangleData (16 words) -- slot t for
+ * triangle t, and for a clipped triangle with several subtriangles slots
+ * header[t].w + k. Host buffers of at least *num_slots slots (any may be
+ * NULL); synchronous. Fails after an overflowing draw. */
+cr_status cr_read_setup_output(cr_context* ctx, uint8_t* tri_subtris, uint32_t* tri_header, uint32_t* tri_data,
+                               int64_t max_slots, int64_t* num_tris, int64_t* num_slots);
+
 /* Fused vertex transform (no counterpart in the reference): while set, the
  * setup stage of cr_draw_triangles / _async takes each vertex's clip position
  * as mvp * (model[i].xyz, 1) -- vertexShader_passthrough (test/shader/

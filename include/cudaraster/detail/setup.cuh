@@ -172,7 +172,6 @@ __device__ __noinline__ void setupClipped(const DrawDev& d, S64 gt, int3 vidx, f
     }
 }
 
-// Resident setup CTAs per SM the compiler must allow (register budget).
 // Clip position of vertex i: its record's clipPos, or, with the fused vertex
 // transform, mvp * (model[i], 1) with each row summed left to right from zero
 // as vertexShader_passthrough (PassThrough.cu:16-35, Math.hpp:990-1001)
@@ -209,7 +208,8 @@ __device__ __forceinline__ void fetchClip(const DrawDev& d, const float4* verts,
     }
 }
 
-// Five resident CTAs per SM (48 registers). Six (40 registers, 52 bytes
+// Resident setup CTAs per SM the compiler must allow (register budget):
+// five (48 registers). Six (40 registers, 52 bytes
 // spilled) measured slower on the soup and the 4x MSAA grid (setup 36.7 ->
 // 38.4 us and 0.168 -> 0.172 ms) and level on the fly-through.
 #ifndef CR_SETUP_MIN_BLOCKS
