@@ -276,10 +276,11 @@ def main():
     ap.add_argument("--profile-frames", type=int, default=0,
                     help="only draw this many frames of the workload (for ncu captures), print nothing else")
     ap.add_argument("--profile-workload", default="soup1m", choices=["soup1m", "subpixel", "flythrough", "flythrough2048",
-                                                              "predicted", "batch64", "textured", "vertex"],
+                                                              "predicted", "batch64", "textured", "vertex", "resolve"],
                     help="workload of --profile-frames: the 1M soup (default), the 4x MSAA heightfield, plain "
                          "fly-through frames, predictor-sized fly-through frames (12 of them, 8 training), "
-                         "replays of the uneven 64-scene batch, textured Phong frames or vertex-shader launches")
+                         "replays of the uneven 64-scene batch, textured Phong frames, vertex-shader launches or "
+                         "MSAA resolves of a 4x 4K surface")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
@@ -301,7 +302,8 @@ def main():
     tuning = workloads.load_tuning("soup1m")
     if args.profile_frames > 0 and args.profile_workload != "soup1m":
         wname = "flythrough" if args.profile_workload.startswith("flythrough") or args.profile_workload == "predicted" \
-            else {"textured": "subpixel", "vertex": "soup1m"}.get(args.profile_workload, args.profile_workload)
+            else {"textured": "subpixel", "vertex": "soup1m", "resolve": "soup1m"}.get(args.profile_workload,
+                                                                                     args.profile_workload)
         print(json.dumps(workloads.profile_frames(args.profile_workload, args.profile_frames,
                                                   workloads.load_tuning(wname))))
         return

@@ -15,23 +15,31 @@
 namespace cr {
 namespace {
 
-__global__ void resolveKernel(const uint32_t* __restrict__ color, int width, int height, int samplesLog2,
-                              int64_t rowWords, uint32_t* __restrict__ out, int64_t outRowWords) {
+// One thread per pixel; the sample count is a template parameter so the
+// sample loads are unrolled and issued together.
+template <int samplesLog2>
+__global__ void resolveKernel(const uint32_t* __restrict__ color, int width, int height, int64_t rowWords,
+                              uint32_t* __restrict__ out, int64_t outRowWords) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= width || y >= height) return;
-    const int ns = 1 << samplesLog2;
+    constexpr int ns = 1 << samplesLog2;
     const int64_t base = (int64_t)y * rowWords + (int64_t)(x >> 3) * 8 * ns + (x & 7);
-    uint32_t sum[4] = {0, 0, 0, 0};
+    // Channels R and B summed in the 16-bit lanes of `rb`, G and A in those of
+    // `ga`: a lane holds at most 8 * 255 + 4 < 2^16, so lanes never carry into
+    // each other, and the bits a right shift moves across a lane boundary are
+    // masked off.
+    uint32_t rb = 0, ga = 0;
+#pragma unroll
     for (int i = 0; i < ns; i++) {
-        const uint32_t c = color[base + i * 8];
-#pragma unroll
-        for (int k = 0; k < 4; k++) sum[k] += (c >> (8 * k)) & 0xFFu;
+        const uint32_t c = __ldg(&color[base + i * 8]);
+        rb += c & 0x00FF00FFu;
+        ga += (c >> 8) & 0x00FF00FFu;
     }
-    uint32_t px = 0;
-#pragma unroll
-    for (int k = 0; k < 4; k++) px |= ((sum[k] + (uint32_t)(ns >> 1)) >> samplesLog2) << (8 * k);
-    out[(int64_t)y * outRowWords + x] = px;
+    constexpr uint32_t half = (uint32_t)(ns >> 1) * 0x00010001u;
+    rb = ((rb + half) >> samplesLog2) & 0x00FF00FFu;
+    ga = ((ga + half) >> samplesLog2) & 0x00FF00FFu;
+    out[(int64_t)y * outRowWords + x] = rb | (ga << 8);
 }
 
 }  // namespace
@@ -47,7 +55,14 @@ extern "C" cr_status cr_resolve_color(const void* color, int32_t width, int32_t 
     while ((1 << log2) < num_samples) log2++;
     const int64_t rowWords = (int64_t)((width + 7) & ~7) * num_samples;
     const dim3 block(32, 8), grid((width + 31) / 32, (height + 7) / 8);
-    cr::resolveKernel<<<grid, block, 0, (cudaStream_t)stream>>>((const uint32_t*)color, width, height, log2, rowWords,
-                                                               (uint32_t*)out, out_row_bytes / 4);
+    const uint32_t* c = (const uint32_t*)color;
+    uint32_t* o = (uint32_t*)out;
+    const cudaStream_t s = (cudaStream_t)stream;
+    switch (log2) {
+    case 0: cr::resolveKernel<0><<<grid, block, 0, s>>>(c, width, height, rowWords, o, out_row_bytes / 4); break;
+    case 1: cr::resolveKernel<1><<<grid, block, 0, s>>>(c, width, height, rowWords, o, out_row_bytes / 4); break;
+    case 2: cr::resolveKernel<2><<<grid, block, 0, s>>>(c, width, height, rowWords, o, out_row_bytes / 4); break;
+    default: cr::resolveKernel<3><<<grid, block, 0, s>>>(c, width, height, rowWords, o, out_row_bytes / 4); break;
+    }
     return cudaGetLastError() == cudaSuccess ? CR_OK : CR_ERR_CUDA;
 }

@@ -527,6 +527,16 @@ def profile_frames(name: str, frames: int, tuning: dict | None = None) -> dict:
     if name == "textured":
         s, _, _, _ = measure_textured(steps=frames, warmup=0, tuning=tuning)
         return {"profile": name, "frames": frames, "counters": s["counters"]}
+    if name == "resolve":   # `frames` resolves of a 4x MSAA 3840x2160 colour surface
+        p = _pkg()
+        raster = importlib.import_module(PKG + ".raster")
+        cs = p.CudaSurface((3840, 2160), p.CudaSurface.FORMAT_RGBA8, 4)
+        g = torch.Generator(device="cuda").manual_seed(9)
+        cs.tensor.copy_(torch.randint(-2**31, 2**31 - 1, cs.tensor.shape, generator=g, device="cuda",
+                                      dtype=torch.int32))
+        ms = time_events(lambda: cs.resolve(), max(frames, 1), torch.cuda.current_stream())
+        return {"profile": name, "frames": frames, "ms": round(float(np.median(ms)), 4),
+                "bytes_per_resolve": 3840 * 2160 * (16 + 4)}
     if name == "vertex":
         v = measure_vertex_shaders(n=8 << 20, steps=frames, warmup=0)   # 268 MB of input records, above L2
         return {"profile": name, "frames": frames, "vertices": v["vertices"]}

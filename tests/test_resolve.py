@@ -57,3 +57,18 @@ def test_resolve_matches_rule(cuda, pipe):
     want = resolve_reference(gc, 333, 250, s)
     assert got.shape == (250, 333, 4)
     np.testing.assert_array_equal(got, want)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("samples", [1, 2, 4, 8])
+def test_resolve_random_words(cuda, samples):
+    # Every byte value in every sample, including all-255 pixels (the largest lane sums).
+    p = pkg()
+    w, h = 203, 77
+    surf = p.CudaSurface((w, h), p.CudaSurface.FORMAT_RGBA8, samples)
+    rng = np.random.default_rng(samples)
+    words = rng.integers(0, 2**32, tuple(surf.tensor.shape), dtype=np.uint64).astype(np.uint32)
+    words[::5] = 0xFFFFFFFF
+    surf.tensor.copy_(torch.from_numpy(words.view(np.int32)))
+    got = surf.resolve().cpu().numpy()
+    np.testing.assert_array_equal(got, resolve_reference(words, w, h, samples))
