@@ -109,7 +109,7 @@ __device__ __forceinline__ F32 crDot(const Vec3f& a, const Vec3f& b) {
 
 __device__ __forceinline__ Vec3f crNormalize(const Vec3f& v) {
     const F32 len = __fsqrt_rn(crDot(v, v));
-    const F32 s = __fmul_rn(1.0f, len != 0.0f ? __fdiv_rn(1.0f, len) : 0.0f);
+    const F32 s = __fmul_rn(1.0f, len != 0.0f ? __frcp_rn(len) : 0.0f);  // 1 / len, correctly rounded
     return Vec3f(__fmul_rn(v.x, s), __fmul_rn(v.y, s), __fmul_rn(v.z, s));
 }
 
