@@ -122,3 +122,24 @@ def test_tex_phong_constants_validation(cuda):
            (m.data_ptr(), 1, t.data_ptr(), 4, None, 2, 2), (m.data_ptr(), 1, t.data_ptr(), 4, a.data_ptr(), 0, 2)]
     for args in bad:
         assert lib.cr_set_tex_phong_constants(*args, None) == 1
+
+
+@pytest.mark.parametrize("tuning", [dict(bin_log2=3, fine_warps=4), dict(bin_log2=5, bin_chunk_tris=96),
+                                    dict(fine_self_pixels=1, coarse_unit_entries=64),
+                                    dict(fine_self_pixels=64, fine_warps=8)])
+def test_textured_tuning_invariance(cuda, tuning):
+    # Tuning changes queues and work distribution, never a bit of the textured frame.
+    p = pkg()
+    raster = pkg_mod("raster")
+    scenes = pkg_mod("scenes")
+    sc = scenes.textured_terrain(96, 512, 384, seed=13)
+    k = [sc["pos_to_clip"], sc["pos_to_camera"], sc["normal_to_camera"]]
+    shaded = raster.vertex_shader_tex_phong(torch.from_numpy(sc["input"]).cuda(), *k).cpu().numpy()
+    raster.set_tex_phong_constants(torch.from_numpy(sc["materials"]).cuda(),
+                                   torch.from_numpy(sc["triangle_material_idx"]).cuda(),
+                                   torch.from_numpy(sc["atlas"].view(np.int32)).cuda())
+    scene = {"vertices": shaded, "indices": sc["indices"], "width": 512, "height": 384}
+    clear = (p.color_to_abgr(0.1, 0.2, 0.3, 1.0), p.clear_depth_from_float(1.0))
+    base = gpu_render("PixelPipe_texPhong", scene, clear)
+    tuned = gpu_render("PixelPipe_texPhong", scene, clear, tuning=tuning)
+    assert_same(tuned[0], tuned[1], base[0], base[1], f"tuning {tuning}")
