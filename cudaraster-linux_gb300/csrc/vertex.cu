@@ -1,10 +1,11 @@
-// vertex.cu -- the vertex stage before the rasterizer: clip = MVP * (model, 1)
-// per vertex, the reference's vertexShader_passthrough (test/shader/
-// PassThrough.cu:16-35) with Mat4f * Vec4f evaluated as the reference's
-// framework writes it (Math.hpp:990-1001: r[i] = sum over j of m(i, j) * v[j],
-// accumulated left to right from zero, each operation rounded on its own).
-// Per-vertex RGBA colours (optional) are copied behind the position to form
-// GouraudVertex records.
+// vertex.cu -- the vertex stage before the rasterizer: the reference's example
+// vertex shaders. vertexShader_passthrough (test/shader/PassThrough.cu:16-35):
+// clip = MVP * (model, 1) per vertex with Mat4f * Vec4f evaluated as the
+// reference's framework writes it (Math.hpp:990-1001: r[i] = sum over j of
+// m(i, j) * v[j], accumulated left to right from zero, each operation rounded
+// on its own); per-vertex RGBA colours (optional) are copied behind the
+// position to form GouraudVertex records. Below it, vertexShader_gouraud and
+// vertexShader_texPhong (Shaders.cu:55-108).
 #include "cudaraster.h"
 #include "cudaraster/ShaderMath.hpp"
 #include "cudaraster/detail/device.cuh"
@@ -44,7 +45,8 @@ __global__ void __launch_bounds__(256) vertexPassthroughKernel(const float* __re
 extern "C" cr_status cr_vertex_shader_passthrough(const float* model, int32_t model_stride, const float* colors,
                                                   int32_t color_stride, void* out_vertices, int32_t out_stride_bytes,
                                                   int64_t num_vertices, const float* mvp_row_major, void* stream) {
-    if (!model || !out_vertices || !mvp_row_major || num_vertices < 0 || model_stride < 3 ||
+    if (!model || !out_vertices || !mvp_row_major || num_vertices < 0 || (num_vertices + 255) / 256 > 0x7FFFFFFF ||
+        model_stride < 3 ||
         (out_stride_bytes != 16 && out_stride_bytes != 32) || (colors && color_stride < 4) ||
         ((uintptr_t)out_vertices & 15))
         return CR_ERR_INVALID_ARGUMENT;
