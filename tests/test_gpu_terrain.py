@@ -30,6 +30,11 @@ def test_vertex_shader_bit_exact(cuda):
     ref = vertex_oracle.vertex_passthrough(model, mvp)
     np.testing.assert_array_equal(got[:, :4].view(np.uint32), ref.view(np.uint32))
     np.testing.assert_array_equal(got[:, 4:], colors)
+    # A 4-float position stride without colours (16-byte records): the same bits.
+    m4 = torch.ones((model.shape[0], 4), dtype=torch.float32, device="cuda")
+    m4[:, :3] = torch.from_numpy(model).cuda()
+    clip_only = raster.vertex_shader_passthrough(m4[:, :3], mvp).cpu().numpy()
+    np.testing.assert_array_equal(clip_only.view(np.uint32), ref.view(np.uint32))
 
 
 def _terrain(n, w, h, samples, frame):
