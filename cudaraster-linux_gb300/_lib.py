@@ -84,6 +84,9 @@ _SIGNATURES = {
     "cr_set_vertex_transform": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
     "cr_read_setup_output": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
                                        C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "cr_read_queue_output": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                                       C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_int64),
+                                       C.POINTER(C.c_int64)]),
     "cr_set_index_buffer": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32]),
     "cr_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
     "cr_set_debug_params": (C.c_int, [C.c_void_p, C.POINTER(DebugParams)]),

@@ -76,16 +76,30 @@ def build_library(force: bool = False, verbose: bool = False, extra: list[str] |
     return LIB_PATH
 
 
+def reference_dir() -> Path | None:
+    """The reference sources (tcoppex/cudaraster-linux checkout) named by the
+    CR_REFERENCE_DIR environment variable, if it is set and holds them."""
+    d = os.environ.get("CR_REFERENCE_DIR")
+    if not d:
+        return None
+    p = Path(d)
+    return p if (p / "src" / "cudaraster" / "cuda" / "PixelPipe.inl").exists() else None
+
+
 def build_oracle(with_reference: bool | None = None) -> None:
-    """Build oracle/liboracle.so, and oracle/_ref when the reference sources exist."""
+    """Build oracle/liboracle.so, and oracle/_ref when CR_REFERENCE_DIR names the
+    reference sources."""
     oracle_dir = REPO_DIR / "oracle"
     res = subprocess.run(["make", "-C", str(oracle_dir), "liboracle.so"], capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{res.stdout}\n{res.stderr}")
+    ref = reference_dir()
     if with_reference is None:
-        with_reference = Path("/root/reference/src/cudaraster/cuda/PixelPipe.inl").exists()
+        with_reference = ref is not None
     if with_reference:
-        res = subprocess.run(["make", "-C", str(oracle_dir), "ref"], capture_output=True, text=True)
+        if ref is None:
+            raise RuntimeError("set CR_REFERENCE_DIR to the reference sources to build oracle/_ref")
+        res = subprocess.run(["make", "-C", str(oracle_dir), "ref", f"REF={ref}"], capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"reference harness build failed:\n{res.stdout}\n{res.stderr}")
 

@@ -27,6 +27,7 @@
 // as in the reference. Placement of a list in memory depends on atomics,
 // its content and order do not.
 #include "cudaraster/detail/binning.cuh"
+#include "cudaraster/detail/per_device.h"
 
 namespace cr {
 
@@ -636,42 +637,43 @@ size_t coarseCountSmem(int binLog2) { return sizeof(S32) * kCoarseWarps * ((size
 size_t coarseScatterSmem(int binLog2) { return sizeof(S32) * kCoarseWarps * ((size_t)1 << (2 * binLog2)); }
 
 cudaError_t launchBinning(const DrawDev& d, int maxBins, int numSMs, cudaStream_t stream, cudaEvent_t evCoarse) {
-    // Resident coarse CTAs per SM for bins of 8, 16 and 32 tiles a side.
-    static int coarseCountCtas[6] = {}, coarseScatterCtas[6] = {};
-    static bool configured = false;
-    if (!configured) {
+    // Shared-memory limits are per device: set them once on each device used.
+    static OncePerDevice attributes;
+    attributes.run([] {
         cudaFuncSetAttribute(binScatterKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
         cudaFuncSetAttribute(binCountKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
         cudaFuncSetAttribute(coarseScatterKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
         cudaFuncSetAttribute(coarseCountKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
         cudaFuncSetAttribute(coarseScanKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
-        for (int b = 3; b <= 5; b++) {
-            int n = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, coarseCountKernel, kCoarseThreads, coarseCountSmem(b));
-            coarseCountCtas[b] = n > 0 ? n : 1;
-            n = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, coarseScatterKernel, kCoarseThreads, coarseScatterSmem(b));
-            coarseScatterCtas[b] = n > 0 ? n : 1;
-        }
-        configured = true;
-    }
+    });
+    // Resident coarse CTAs per SM for bins of 8, 16 and 32 tiles a side.
+    static IntsPerDevice<6> coarseCountCtas, coarseScatterCtas;
     const int bl = d.binLog2 >= 3 && d.binLog2 <= 5 ? d.binLog2 : 4;
+    const int countCtas = coarseCountCtas.get(bl, [](int b) {
+        int n = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, coarseCountKernel, kCoarseThreads, coarseCountSmem(b));
+        return n > 0 ? n : 1;
+    });
+    const int scatterCtas = coarseScatterCtas.get(bl, [](int b) {
+        int n = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, coarseScatterKernel, kCoarseThreads, coarseScatterSmem(b));
+        return n > 0 ? n : 1;
+    });
     // Units sized on the device: about two per resident coarse-scatter warp.
     DrawDev dl = d;
-    dl.unitTarget = 2 * numSMs * coarseScatterCtas[bl] * kCoarseWarps;
+    dl.unitTarget = 2 * numSMs * scatterCtas * kCoarseWarps;
     // binScan also runs for a draw without triangles: it zeroes the bin counts.
     // Persistent bin warps: as many CTAs as are resident at once, and no more
     // than the draw's chunks can keep busy.
     dl.maxBins = maxBins;
     const int walkSmem = (int)binWalkSmem(maxBins);
-    static int walkCtasFor[1025] = {};   // resident bin CTAs per SM, by bins of the largest instance
+    static IntsPerDevice<1025> walkCtasFor;   // resident bin CTAs per SM, by bins of the largest instance
     const int mb = maxBins >= 1 && maxBins <= 1024 ? maxBins : 1024;
-    if (walkCtasFor[mb] == 0) {
+    const int walkCtas = walkCtasFor.get(mb, [](int bins) {
         int n = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, binScatterKernel, kWalkThreads, walkSmem);
-        walkCtasFor[mb] = n > 0 ? n : 1;
-    }
-    const int walkCtas = walkCtasFor[mb];
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, binScatterKernel, kWalkThreads, (int)binWalkSmem(bins));
+        return n > 0 ? n : 1;
+    });
     const int walkGrid = (int)min((S64)numSMs * walkCtas, (S64)(dl.totalChunks + kWalkWarps - 1) / kWalkWarps);
     if (dl.totalChunks > 0) binCountKernel<<<walkGrid, kWalkThreads, walkSmem, stream>>>(dl);
     binScanKernel<<<dl.totalBins, kBinThreads, 0, stream>>>(dl);
@@ -680,8 +682,8 @@ cudaError_t launchBinning(const DrawDev& d, int maxBins, int numSMs, cudaStream_
     // Persistent coarse warps: as many CTAs as are resident at once, and no
     // more than the draw's units can keep busy.
     const S64 unitCtas = (dl.maxUnits + kCoarseWarps - 1) / kCoarseWarps;
-    const int countGrid = (int)min((S64)numSMs * coarseCountCtas[bl], unitCtas);
-    const int scatterGrid = (int)min((S64)numSMs * coarseScatterCtas[bl], unitCtas);
+    const int countGrid = (int)min((S64)numSMs * countCtas, unitCtas);
+    const int scatterGrid = (int)min((S64)numSMs * scatterCtas, unitCtas);
     coarseCountKernel<<<countGrid, kCoarseThreads, coarseCountSmem(dl.binLog2), stream>>>(dl);
     coarseScanKernel<<<dl.totalBins, kBinThreads, sizeof(S32) * kBinWarps * ((size_t)1 << (2 * dl.binLog2)), stream>>>(dl);
     coarseScatterKernel<<<scatterGrid, kCoarseThreads, coarseScatterSmem(dl.binLog2), stream>>>(dl);

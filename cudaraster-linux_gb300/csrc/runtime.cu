@@ -359,6 +359,37 @@ cr_status cr_read_setup_output(cr_context* ctx, uint8_t* tri_subtris, uint32_t* 
     return CR_OK;
 }
 
+cr_status cr_read_queue_output(cr_context* ctx, int32_t* bin_start, int32_t* bin_count, uint32_t* bin_list,
+                               int64_t max_bin_entries, int32_t* tile_start, int32_t* tile_count,
+                               uint32_t* tile_list, int64_t max_tile_entries, int64_t* num_bin_entries,
+                               int64_t* num_tile_entries) {
+    if (!ctx || !num_bin_entries || !num_tile_entries || max_bin_entries < 0 || max_tile_entries < 0)
+        return CR_ERR_INVALID_ARGUMENT;
+    if (ctx->lastLayout.num_instances != 1)
+        return fail(ctx, CR_ERR_INVALID_STATE, "CudaRaster: queue output is kept for single draws only");
+    cr_counters c;
+    cr_status st = cr_get_counters(ctx, &c);
+    if (st != CR_OK) return st;
+    *num_bin_entries = c.bin_entries;
+    *num_tile_entries = c.tile_entries;
+    if (c.overflow) return fail(ctx, CR_ERR_INVALID_STATE, "CudaRaster: the last draw overflowed");
+    if ((bin_list && c.bin_entries > max_bin_entries) || (tile_list && c.tile_entries > max_tile_entries))
+        return fail(ctx, CR_ERR_CAPACITY, "CudaRaster: %lld bin / %lld tile entries do not fit",
+                    (long long)c.bin_entries, (long long)c.tile_entries);
+    CR_CUDA(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+    const size_t nb = (size_t)c.num_bins, nt = (size_t)c.num_tiles;
+    if (bin_start) CR_CUDA(cudaMemcpy(bin_start, ctx->binStart.ptr, nb * 4, cudaMemcpyDeviceToHost), "cudaMemcpy");
+    if (bin_count) CR_CUDA(cudaMemcpy(bin_count, ctx->binCount.ptr, nb * 4, cudaMemcpyDeviceToHost), "cudaMemcpy");
+    if (tile_start) CR_CUDA(cudaMemcpy(tile_start, ctx->tileStart.ptr, nt * 4, cudaMemcpyDeviceToHost), "cudaMemcpy");
+    if (tile_count) CR_CUDA(cudaMemcpy(tile_count, ctx->tileCount.ptr, nt * 4, cudaMemcpyDeviceToHost), "cudaMemcpy");
+    if (bin_list && c.bin_entries > 0)
+        CR_CUDA(cudaMemcpy(bin_list, ctx->binList.ptr, (size_t)c.bin_entries * 4, cudaMemcpyDeviceToHost), "cudaMemcpy");
+    if (tile_list && c.tile_entries > 0)
+        CR_CUDA(cudaMemcpy(tile_list, ctx->tileList.ptr, (size_t)c.tile_entries * 4, cudaMemcpyDeviceToHost),
+                "cudaMemcpy");
+    return CR_OK;
+}
+
 cr_status cr_set_vertex_transform(cr_context* ctx, const float* model, int32_t model_stride,
                                   const float* mvp_row_major) {
     if (!ctx) return CR_ERR_INVALID_ARGUMENT;

@@ -169,6 +169,22 @@ cr_status cr_set_vertex_buffer(cr_context* ctx, const void* vertices, int64_t of
 cr_status cr_read_setup_output(cr_context* ctx, uint8_t* tri_subtris, uint32_t* tri_header, uint32_t* tri_data,
                                int64_t max_slots, int64_t* num_tris, int64_t* num_slots);
 
+/* Inspection of the last single draw's bin and tile queues (the intermediate
+ * lists the reference exposed only through its host emulation of the bin and
+ * coarse stages, CudaRaster.hpp:53-67, BinRaster.inl:381-418,
+ * CoarseRaster.inl:561-680): for every bin (row-major over the viewport's
+ * bins of 8 << bin_log2 pixels) the start and length of its list in
+ * bin_list, likewise for every 8x8 tile in tile_list. Entries are
+ * triangle << 3 | subtriangle (7 = the triangle's only subtriangle) in
+ * submission order. Host buffers: bin_start / bin_count of num_bins entries,
+ * tile_start / tile_count of num_tiles (cr_get_counters), the lists of at
+ * least *num_bin_entries / *num_tile_entries words (any pointer may be NULL to
+ * query the sizes). Synchronous. Fails after an overflowing draw or a batch. */
+cr_status cr_read_queue_output(cr_context* ctx, int32_t* bin_start, int32_t* bin_count, uint32_t* bin_list,
+                               int64_t max_bin_entries, int32_t* tile_start, int32_t* tile_count,
+                               uint32_t* tile_list, int64_t max_tile_entries, int64_t* num_bin_entries,
+                               int64_t* num_tile_entries);
+
 /* Fused vertex transform (no counterpart in the reference): while set, the
  * setup stage of cr_draw_triangles / _async takes each vertex's clip position
  * as mvp * (model[i].xyz, 1) -- vertexShader_passthrough (test/shader/

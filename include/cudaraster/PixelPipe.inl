@@ -13,6 +13,7 @@
 
 #include "PixelPipe.hpp"
 #include "detail/fine.cuh"
+#include "detail/per_device.h"
 #include "detail/pipe_registry.h"
 #include "detail/setup.cuh"
 
@@ -42,11 +43,7 @@ struct PipeImpl {
                                   int ctasPerSM, int numSMs, cudaStream_t stream) {
         if (tileEnd <= tileBegin) return cudaSuccess;
         auto kern = fineKernelFor<V, FS, BS, S, F>();
-        static bool configured = false;
-        if (!configured) {
-            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-            configured = true;
-        }
+        configureFine();
         int64_t warpsNeeded = tileEnd - tileBegin;
         int64_t grid = (int64_t)numSMs * ctasPerSM;
         int64_t maxGrid = (warpsNeeded + warps - 1) / warps;
@@ -55,18 +52,26 @@ struct PipeImpl {
         kern<<<(unsigned)grid, warps * 32, smemBytes(warps), stream>>>(d, group, tileBegin, tileEnd);
         return cudaGetLastError();
     }
-    // Resident fine CTAs per SM, by warps per CTA (queried once per size).
+    // The fine kernel's shared-memory limit, set once on each device used.
+    static void configureFine() {
+        static OncePerDevice once;
+        once.run([] {
+            cudaFuncSetAttribute(fineKernelFor<V, FS, BS, S, F>(), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 160 * 1024);
+        });
+    }
+    // Resident fine CTAs per SM, by warps per CTA (queried once per size and device).
     static int fineOccupancy(int warps) {
-        static int cache[9] = {};
+        static IntsPerDevice<9> cache;
         const int w = warps >= 1 && warps <= 8 ? warps : 8;
-        if (cache[w] > 0) return cache[w];
-        auto kern = fineKernelFor<V, FS, BS, S, F>();
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-        int blocks = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, w * 32, smemBytes(w)) != cudaSuccess)
-            return 1;
-        cache[w] = blocks > 0 ? blocks : 1;
-        return cache[w];
+        configureFine();
+        return cache.get(w, [](int ww) {
+            int blocks = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fineKernelFor<V, FS, BS, S, F>(), ww * 32,
+                                                              smemBytes(ww)) != cudaSuccess)
+                return 1;
+            return blocks > 0 ? blocks : 1;
+        });
     }
     static void describe(PipeDesc& p, const char* name, const char* blend, const char* frag) {
         memset(&p, 0, sizeof(p));

@@ -742,6 +742,41 @@ inline S64 surface_index(const or_pipe* p, S32 x, S32 y, int i) {
 
 }  // namespace
 
+namespace {
+struct QItem { U32 entry; TriGeom g; };
+
+bool edge_touches_rect(S64 ox, S64 oy, S64 dx, S64 dy, S64 rx0, S64 ry0, S64 rx1, S64 ry1) {
+    S64 px = dy > 0 ? rx0 : rx1;
+    S64 py = dx > 0 ? ry1 : ry0;
+    return (ox - px) * dy - (oy - py) * dx >= 0;
+}
+
+bool tri_touches_rect(const TriGeom& g, S64 rx0, S64 ry0, S64 rx1, S64 ry1) {
+    return edge_touches_rect(g.v0x, g.v0y, g.v1x - g.v0x, g.v1y - g.v0y, rx0, ry0, rx1, ry1) &&
+           edge_touches_rect(g.v1x, g.v1y, g.v2x - g.v1x, g.v2y - g.v1y, rx0, ry0, rx1, ry1) &&
+           edge_touches_rect(g.v2x, g.v2y, g.v0x - g.v2x, g.v0y - g.v2y, rx0, ry0, rx1, ry1);
+}
+
+// Cells of the rule in the window [wx0, wx1] x [wy0, wy1] of a grid with cells
+// of 2^cellLog2 subpixels.
+template <class Fn>
+void rule_cells(const Viewport& vp, const TriGeom& g, int cellLog2, S32 wx0, S32 wy0, S32 wx1, S32 wy1, Fn fn) {
+    const S32 hw = vp.width << (SUBPIXEL_LOG2 - 1), hh = vp.height << (SUBPIXEL_LOG2 - 1);
+    S32 lx = std::max((min3(g.v0x, g.v1x, g.v2x) + hw) >> cellLog2, wx0);
+    S32 hx = std::min((max3(g.v0x, g.v1x, g.v2x) + hw) >> cellLog2, wx1);
+    S32 ly = std::max((min3(g.v0y, g.v1y, g.v2y) + hh) >> cellLog2, wy0);
+    S32 hy = std::min((max3(g.v0y, g.v1y, g.v2y) + hh) >> cellLog2, wy1);
+    if (lx > hx || ly > hy) return;
+    const bool small = hx - lx <= 1 && hy - ly <= 1;
+    const S64 side = (S64)1 << cellLog2;
+    for (S32 cy = ly; cy <= hy; cy++)
+        for (S32 cx = lx; cx <= hx; cx++) {
+            const S64 rx0 = ((S64)cx << cellLog2) - hw, ry0 = ((S64)cy << cellLog2) - hh;
+            if (small || tri_touches_rect(g, rx0, ry0, rx0 + side - 1, ry0 + side - 1)) fn(cx, cy);
+        }
+}
+}  // namespace
+
 // ===================================================================== C API
 
 extern "C" {
@@ -944,6 +979,94 @@ int or_render(const or_pipe* p, const float* vertices, const int32_t* indices,
         stats->tile_entries = entries;
     }
     return 0;
+}
+
+// Per-stage queue model: the bin and tile lists of one draw, by cell, as
+// CSR arrays. Entries are triangle << 3 | subtriangle (7 when the triangle has
+// one subtriangle: BinRaster.inl:148-158), in submission order.
+//   kind 0 / 2: bins / tiles, exact -- entries covering at least one sample of
+//               the cell's pixels (the per-sample rule above);
+//   kind 1 / 3: bins / tiles, the binning rule of the GPU stages -- the
+//               entry's bounding box, in cells and clamped to the cell window
+//               (the viewport's bins; for tiles the tiles of the bin), contains
+//               the cell, and either the clamped box spans at most 2x2 cells or
+//               no edge has the whole cell rectangle strictly outside; a tile
+//               only takes entries of its bin's list. The reference bins
+//               conservatively in the same sense (BinRaster.inl:228-300,
+//               CoarseRaster.inl:299-435).
+// Fills offsets[num_cells + 1] and entries[] when the total fits `cap`;
+// returns the total (-1 on bad arguments).
+
+int64_t or_queue_lists(const or_pipe* p, const float* vertices, const int32_t* indices, int64_t num_tris,
+                       int bin_log2, int kind, int64_t* offsets, uint32_t* entries, int64_t cap) {
+    if (bin_log2 < 3 || bin_log2 > 5 || kind < 0 || kind > 3) return -1;
+    Viewport vp{p->width, p->height};
+    const int s = p->samples_log2;
+    const int stride4 = p->vertex_stride / 16;
+    std::vector<TriSetup> res((size_t)std::max<int64_t>(num_tris, 0));
+#pragma omp parallel for schedule(static)
+    for (int64_t t = 0; t < num_tris; t++)
+        setup_one(vp, s, p->render_mode, vertices, stride4, &indices[t * 3], res[t]);
+    std::vector<QItem> items;
+    for (int64_t t = 0; t < num_tris; t++)
+        for (int i = 0; i < res[t].num; i++)
+            items.push_back({(U32)(t << 3) | (U32)(res[t].num == 1 ? 7 : i), geom_from_header(res[t].sub[i].h)});
+    const S32 wt = (p->width + 7) >> 3, ht = (p->height + 7) >> 3;
+    const S32 side = 1 << bin_log2;
+    const S32 wb = (wt + side - 1) / side, hb = (ht + side - 1) / side;
+    const bool bins = kind < 2, exact = (kind & 1) == 0;
+    const S64 numCells = bins ? (S64)wb * hb : (S64)wt * ht;
+    std::vector<std::vector<U32>> lists((size_t)numCells);
+    const int tileCell = SUBPIXEL_LOG2 + TILE_LOG2, binCell = tileCell + bin_log2;
+    for (const QItem& it : items) {
+        if (exact) {
+            // Every tile whose pixels hold a covered sample (boxes clamped to the viewport's tiles).
+            const S32 hw = vp.width << (SUBPIXEL_LOG2 - 1), hh = vp.height << (SUBPIXEL_LOG2 - 1);
+            S32 lx = std::max((min3(it.g.v0x, it.g.v1x, it.g.v2x) + hw) >> tileCell, 0);
+            S32 hx = std::min((max3(it.g.v0x, it.g.v1x, it.g.v2x) + hw) >> tileCell, wt - 1);
+            S32 ly = std::max((min3(it.g.v0y, it.g.v1y, it.g.v2y) + hh) >> tileCell, 0);
+            S32 hy = std::min((max3(it.g.v0y, it.g.v1y, it.g.v2y) + hh) >> tileCell, ht - 1);
+            for (S32 ty = ly; ty <= hy; ty++)
+                for (S32 tx = lx; tx <= hx; tx++) {
+                    bool hit = false;
+                    for (int pi = 0; pi < 64 && !hit; pi++)
+                        hit = sample_mask(vp, s, it.g, tx * 8 + (pi & 7), ty * 8 + (pi >> 3)) != 0;
+                    if (!hit) continue;
+                    if (!bins) {
+                        lists[(size_t)ty * wt + tx].push_back(it.entry);
+                    } else {
+                        std::vector<U32>& l = lists[(size_t)(ty >> bin_log2) * wb + (tx >> bin_log2)];
+                        if (l.empty() || l.back() != it.entry) l.push_back(it.entry);
+                    }
+                }
+        } else {
+            rule_cells(vp, it.g, binCell, 0, 0, wb - 1, hb - 1, [&](S32 bx, S32 by) {
+                if (bins) {
+                    lists[(size_t)by * wb + bx].push_back(it.entry);
+                    return;
+                }
+                const S32 x0 = bx << bin_log2, y0 = by << bin_log2;
+                rule_cells(vp, it.g, tileCell, x0, y0, std::min(x0 + side - 1, wt - 1), std::min(y0 + side - 1, ht - 1),
+                           [&](S32 tx, S32 ty) { lists[(size_t)ty * wt + tx].push_back(it.entry); });
+            });
+        }
+    }
+    if (exact && bins)
+        for (auto& l : lists) {   // an entry's tiles of one bin are not consecutive in row order
+            std::sort(l.begin(), l.end());
+            l.erase(std::unique(l.begin(), l.end()), l.end());
+        }
+    int64_t total = 0;
+    for (const auto& l : lists) total += (int64_t)l.size();
+    if (total <= cap && offsets && (entries || total == 0)) {
+        int64_t o = 0;
+        for (S64 c = 0; c < numCells; c++) {
+            offsets[c] = o;
+            for (U32 e : lists[(size_t)c]) entries[o++] = e;
+        }
+        offsets[numCells] = o;
+    }
+    return total;
 }
 
 int32_t or_f32_to_s32_sat(float a) { return cvt_rni_sat_s32(a); }

@@ -82,6 +82,16 @@ int or_render(const or_pipe* p, const float* vertices, const int32_t* indices,
               int64_t num_tris, uint32_t* color, uint32_t* depth,
               int num_threads, or_stats* stats);
 
+/* Per-stage queue model of one draw (bins of 8 << bin_log2 pixels, 8x8 tiles)
+ * as CSR arrays over cells in row-major order: kind 0 / 2 = the exact bin /
+ * tile lists (entries covering a sample of the cell), kind 1 / 3 = the lists
+ * the GPU's conservative binning rule keeps. Entries are triangle << 3 |
+ * subtriangle (7 = the triangle's only subtriangle) in submission order.
+ * offsets has num_cells + 1 entries; both arrays are filled only when the
+ * total fits cap. Returns the total, or -1 on bad arguments. */
+int64_t or_queue_lists(const or_pipe* p, const float* vertices, const int32_t* indices, int64_t num_tris,
+                       int bin_log2, int kind, int64_t* offsets, uint32_t* entries, int64_t cap);
+
 /* ---- Single-function entry points used by the known-answer tests. ---- */
 int32_t  or_f32_to_s32_sat(float a);
 uint32_t or_f32_to_u32_sat(float a);

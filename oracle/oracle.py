@@ -76,6 +76,8 @@ def load():
             ("or_tex_normalize_mismatches", C.c_int64, []),
             ("or_log2_exact", C.c_float, [C.c_float]),
             ("or_evaluate_lighting", None, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p]),
+            ("or_queue_lists", C.c_int64, [C.POINTER(Pipe), C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_int,
+                                           C.c_void_p, C.c_void_p, C.c_int64]),
         ]:
             fn = getattr(lib, name)
             fn.restype = res
@@ -97,6 +99,13 @@ def make_pipe(width, height, samples=1, flags=DEPTH | LERP, blend="replace", sha
         p.deferred_clear = 1
         p.clear_color, p.clear_depth = clear
     return p
+
+
+def clear_values(rgba=(0.2, 0.4, 0.8, 1.0), depth=1.0):
+    """(ABGR8 colour, encoded depth) of a deferred clear, by the oracle's restatement of the
+    reference's host arithmetic (Math.cpp:41-48, CudaRaster.cpp:174-179)."""
+    lib = load()
+    return int(lib.or_host_to_abgr(*[float(c) for c in rgba])), int(lib.or_clear_depth(float(depth)))
 
 
 def surface_shape(width, height, samples):
@@ -130,6 +139,30 @@ def setup(pipe: Pipe, vertices: np.ndarray, indices: np.ndarray, max_subtris: in
     used = lib.or_setup(C.byref(pipe), v.ctypes.data, i.ctypes.data, t, sub.ctypes.data, hdr.ctypes.data,
                         dat.ctypes.data, ms)
     return sub, hdr, dat, used
+
+
+QUEUE_KINDS = {"bin_exact": 0, "bin_rule": 1, "tile_exact": 2, "tile_rule": 3}
+
+
+def queue_lists(pipe: Pipe, vertices: np.ndarray, indices: np.ndarray, bin_log2: int, kind: str):
+    """Per-cell bin or tile lists of a draw as (offsets [cells + 1], entries) int64 / uint32
+    arrays (cells in row-major order): "bin_exact" / "tile_exact" hold the entries that
+    cover a sample of the cell, "bin_rule" / "tile_rule" those the GPU binning rule keeps."""
+    lib = load()
+    v = np.ascontiguousarray(vertices, dtype=np.float32)
+    i = np.ascontiguousarray(indices, dtype=np.int32)
+    k = QUEUE_KINDS[kind]
+    total = lib.or_queue_lists(C.byref(pipe), v.ctypes.data, i.ctypes.data, i.shape[0], bin_log2, k, None, None, 0)
+    if total < 0:
+        raise ValueError("bad queue-list arguments")
+    wt, ht = (pipe.width + 7) >> 3, (pipe.height + 7) >> 3
+    side = 1 << bin_log2
+    cells = ((wt + side - 1) // side) * ((ht + side - 1) // side) if k < 2 else wt * ht
+    off = np.zeros(cells + 1, np.int64)
+    ent = np.zeros(max(total, 1), np.uint32)
+    lib.or_queue_lists(C.byref(pipe), v.ctypes.data, i.ctypes.data, i.shape[0], bin_log2, k, off.ctypes.data,
+                       ent.ctypes.data, total)
+    return off, ent[:total]
 
 
 _tex_phong_keep = None

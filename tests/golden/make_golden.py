@@ -1,9 +1,10 @@
 """Generates the golden fixtures in this directory from the reference's own
 device code, compiled for the host by oracle/Makefile (target `ref`, output
-oracle/_ref/libcrref.so; needs the reference sources, so this script runs
-where they are mounted, not on the GPU machine).
+oracle/_ref/libcrref.so; needs the reference sources, named by the
+CR_REFERENCE_DIR environment variable, so this script runs where they are
+mounted, not on the GPU machine).
 
-    make -C oracle ref && python tests/golden/make_golden.py
+    CR_REFERENCE_DIR=<reference checkout> make -C oracle ref && python tests/golden/make_golden.py
 
 Fixtures (npz, seeded inputs + the reference's outputs):
   ref_setup.npz     triangle setup of several scenes (headers, data, subtri counts)
@@ -105,7 +106,7 @@ def shaders(ref):
 
 def main():
     if not orc.ref_available():
-        sys.exit("oracle/_ref/libcrref.so is missing: run `make -C oracle ref` where the reference sources are")
+        sys.exit("oracle/_ref/libcrref.so is missing: run `make -C oracle ref` with CR_REFERENCE_DIR set to the reference sources")
     ref = orc.load_ref()
     if sys.argv[1:] == ["shaders"]:
         shaders(ref)

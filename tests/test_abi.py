@@ -4,6 +4,7 @@ import ctypes as C
 import re
 from pathlib import Path
 
+import numpy as np
 import pytest
 
 from conftest import pkg_mod
@@ -61,6 +62,19 @@ def test_host_helpers_match_reference_host_code(lib):
         assert lib.cr_decode_depth(int(v)) == d
     assert lib.cr_clear_depth_from_float(1.0) == lib.cr_encode_depth(0xFFFFFFFF)
     assert lib.cr_clear_depth_from_float(0.0) == lib.cr_encode_depth(0)
+
+
+def test_oracle_clear_values_match_library(lib):
+    """The oracle's clear-value helpers (used where the product library must not be
+    loaded, e.g. the CPU baseline) equal the library's host arithmetic."""
+    from oracle import oracle as orc
+    rng = np.random.default_rng(7)
+    for rgba in [(0.2, 0.4, 0.8, 1.0), (0.0, 0.0, 0.0, 0.0), (1.0, 1.0, 1.0, 1.0)] + \
+            [tuple(rng.uniform(-0.2, 1.2, 4)) for _ in range(200)]:
+        d = float(rgba[0])
+        c, z = orc.clear_values(rgba, d)
+        assert c == lib.cr_color_to_abgr(*map(float, rgba))
+        assert z == lib.cr_clear_depth_from_float(d)
 
 
 def test_status_strings(lib):
