@@ -91,6 +91,7 @@ _SIGNATURES = {
     "cr_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
     "cr_set_debug_params": (C.c_int, [C.c_void_p, C.POINTER(DebugParams)]),
     "cr_set_capacity": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64]),
+    "cr_set_stage_timing": (C.c_int, [C.c_void_p, C.c_int32]),
     "cr_draw_triangles": (C.c_int, [C.c_void_p, C.c_void_p]),
     "cr_draw_triangles_async": (C.c_int, [C.c_void_p, C.c_void_p]),
     "cr_draw_batch": (C.c_int, [C.c_void_p, C.POINTER(Instance), C.c_int32, C.c_void_p]),

@@ -27,6 +27,7 @@
 // as in the reference. Placement of a list in memory depends on atomics,
 // its content and order do not.
 #include "cudaraster/detail/binning.cuh"
+#include "cudaraster/detail/launch.h"
 #include "cudaraster/detail/per_device.h"
 
 namespace cr {
@@ -65,8 +66,8 @@ struct Grid {
 struct GroupSmem {
     S32 incl[32];   // inclusive prefix of the entries' box tile counts
     U32 v[3][32];   // vertices, packed as in the triangle header
-    U32 box[32];    // lx | ly << 8 | w << 16 (local cells), bit 31: box of at most 2x2 cells
-    U32 mul[32];    // ceil(2^20 / w): tile k of the box is in row (k * mul) >> 20
+    U32 box[32];    // lx | ly << 9 | (w - 1) << 18 (local cells, < 512 each), bit 31: box of at most 2x2 cells
+    U32 mul[32];    // ceil(2^32 / w) (0 for w = 1): cell k of the box is in row umulhi(k, mul)
     U32 entry[32];
 };
 
@@ -96,8 +97,8 @@ __device__ __forceinline__ S32 stageItems(const DrawDev& d, const Grid& gr, bool
     U32 box = 0, mul = 0;
     if (n > 0) {
         const U32 w = (U32)(b.hx - b.lx + 1);
-        box = (U32)(b.lx - gr.cx0) | (U32)(b.ly - gr.cy0) << 8 | w << 16 | (b.small() ? 1u << 31 : 0u);
-        mul = ((1u << 20) + w - 1u) / w;
+        box = (U32)(b.lx - gr.cx0) | (U32)(b.ly - gr.cy0) << 9 | (w - 1u) << 18 | (b.small() ? 1u << 31 : 0u);
+        mul = w > 1u ? 0xFFFFFFFFu / w + 1u : 0u;
     }
     incl = warpInclusiveScan(n);
     gs.incl[lane] = incl;
@@ -113,7 +114,8 @@ __device__ __forceinline__ S32 stageItems(const DrawDev& d, const Grid& gr, bool
 // Pair p of the group (p below the group's pair count): its item j and its
 // cell in the grid's local index space; returns whether the item's triangle
 // may touch the cell (always, for boxes of at most 2x2 cells). The quotient
-// k / w is exact for k < 2^10 and w <= 64 (error below 2^-10).
+// k / w = umulhi(k, ceil(2^32 / w)) is exact for k * w < 2^32 (boxes have at
+// most 512 x 512 cells).
 __device__ __forceinline__ bool pairCell(const GroupSmem& gs, const Grid& gr, S32 p, int& j, int& cell) {
     int jj = 0;
 #pragma unroll
@@ -121,10 +123,11 @@ __device__ __forceinline__ bool pairCell(const GroupSmem& gs, const Grid& gr, S3
         if (gs.incl[jj + s - 1] <= p) jj += s;
     const S32 k = p - (jj ? gs.incl[jj - 1] : 0);
     const U32 box = gs.box[jj];
-    const S32 w = (S32)((box >> 16) & 0xFFu);
-    const S32 q = (S32)(((U32)k * gs.mul[jj]) >> 20);
-    const S32 lx = (S32)(box & 0xFFu) + k - q * w;
-    const S32 ly = (S32)((box >> 8) & 0xFFu) + q;
+    const S32 w = (S32)((box >> 18) & 0x1FFu) + 1;
+    const U32 mul = gs.mul[jj];
+    const S32 q = mul ? (S32)__umulhi((U32)k, mul) : k;
+    const S32 lx = (S32)(box & 0x1FFu) + k - q * w;
+    const S32 ly = (S32)((box >> 9) & 0x1FFu) + q;
     j = jj;
     cell = ly * gr.stride + lx;
     if (box >> 31) return true;
@@ -221,13 +224,13 @@ __device__ __forceinline__ void walkSlice(const DrawDev& d, const Grid& gr, S64 
         const S32 P = stageItems(d, gr, valid, entry, gs, incl, cell1);
         if (P < 0) {
             const bool hit = cell1 >= 0;
-            fn(hit, cell1, lane, __match_any_sync(0xFFFFFFFFu, hit ? (U32)cell1 : 0x10000u + (U32)lane));
+            fn(hit, cell1, lane, __match_any_sync(0xFFFFFFFFu, hit ? (U32)cell1 : 0x80000000u + (U32)lane));
         }
         for (S32 base = 0; base < P; base += 32) {
             const S32 p = base + lane;
             int j = 0, cell = 0;
             const bool hit = p < P && pairCell(gs, gr, p, j, cell);
-            const U32 peers = __match_any_sync(0xFFFFFFFFu, hit ? (U32)cell : 0x10000u + (U32)lane);
+            const U32 peers = __match_any_sync(0xFFFFFFFFu, hit ? (U32)cell : 0x80000000u + (U32)lane);
             fn(hit, cell, j, peers);
         }
         __syncwarp();
@@ -259,6 +262,8 @@ __device__ __forceinline__ ChunkInfo chunkInfo(const DrawDev& d, int chunk) {
 // Persistent warps over chunks: each chunk's entry count per bin, written to
 // the (bin, chunk) matrix where not zero (the matrix is zero between draws).
 __global__ void __launch_bounds__(kWalkThreads) binCountKernel(DrawDev d) {
+    pdlWait();
+    pdlTrigger();
     extern __shared__ S32 s_cells[];   // [kWalkWarps][maxBins]
     __shared__ U32 s_ring[kWalkWarps][kRing];
     __shared__ GroupSmem s_group[kWalkWarps];
@@ -317,6 +322,8 @@ __device__ __forceinline__ void planUnits(const DrawDev& d, S32* s_scratch) {
 // One CTA per global bin: chunk-order exclusive offsets and list allocation;
 // the last CTA to finish plans the coarse units.
 __global__ void __launch_bounds__(kBinThreads) binScanKernel(DrawDev d) {
+    pdlWait();
+    pdlTrigger();
     __shared__ S32 s_scratch[kBinWarps + 1];
     __shared__ int s_inst;
     __shared__ bool s_last;
@@ -371,6 +378,8 @@ __global__ void __launch_bounds__(kBinThreads) binScanKernel(DrawDev d) {
 // Persistent warps over chunks: writes each chunk's entries into the bin
 // lists, from the chunk's offset in every bin it touches.
 __global__ void __launch_bounds__(kWalkThreads) binScatterKernel(DrawDev d) {
+    pdlWait();
+    pdlTrigger();
     extern __shared__ S32 s_cells[];   // [kWalkWarps][maxBins]: next list index per bin
     __shared__ U32 s_ring[kWalkWarps][kRing];
     __shared__ GroupSmem s_group[kWalkWarps];
@@ -451,6 +460,8 @@ __device__ __forceinline__ Grid tileGrid(const UnitInfo& ui, int binLog2) {
 
 // Persistent warps over coarse units (taken dynamically): per-unit tile counts.
 __global__ void __launch_bounds__(kCoarseThreads) coarseCountKernel(DrawDev d) {
+    pdlWait();
+    pdlTrigger();
     extern __shared__ S32 smem[];
     __shared__ GroupSmem s_group[kCoarseWarps];
     if (__ldg(&d.counters->overflow) & (kOverflowSubtris | kOverflowBin)) return;
@@ -491,6 +502,8 @@ __global__ void __launch_bounds__(kCoarseThreads) coarseCountKernel(DrawDev d) {
 // its slice per tile, the slice sums are scanned across warps per tile, and
 // each warp then writes its slice's running offsets.
 __global__ void __launch_bounds__(kBinThreads) coarseScanKernel(DrawDev d) {
+    pdlWait();
+    pdlTrigger();
     extern __shared__ S32 s_part[];   // [kBinWarps][tpb]: slice sums, then slice starts
     __shared__ S32 s_scratch[kBinWarps + 1];
     __shared__ int s_inst;
@@ -570,6 +583,8 @@ __global__ void __launch_bounds__(kBinThreads) coarseScanKernel(DrawDev d) {
 // of a pair in its tile list is the tile's running index plus the number of
 // lower lanes of the batch on the same tile (a match on the tile index).
 __global__ void __launch_bounds__(kCoarseThreads) coarseScatterKernel(DrawDev d) {
+    pdlWait();
+    pdlTrigger();
     extern __shared__ S32 smem[];
     __shared__ GroupSmem s_group[kCoarseWarps];
     if (__ldg(&d.counters->overflow) & (kOverflowSubtris | kOverflowBin | kOverflowTile)) return;
@@ -604,7 +619,7 @@ __global__ void __launch_bounds__(kCoarseThreads) coarseScatterKernel(DrawDev d)
             const S32 P = stageItems(d, gr, valid, valid ? __ldg(&d.binList[e0 + lane]) : 0u, gs, incl, cell1);
             if (P < 0) {
                 const bool hit = cell1 >= 0;
-                const U32 peers = __match_any_sync(0xFFFFFFFFu, hit ? (U32)cell1 : 0x10000u + (U32)lane);
+                const U32 peers = __match_any_sync(0xFFFFFFFFu, hit ? (U32)cell1 : 0x80000000u + (U32)lane);
                 if (hit) {
                     const S64 idx = (S64)run[cell1] + __popc(peers & ltMask);
                     if (idx < d.maxTileEntries) d.tileList[idx] = gs.entry[lane];
@@ -617,7 +632,7 @@ __global__ void __launch_bounds__(kCoarseThreads) coarseScatterKernel(DrawDev d)
                 const S32 p = base + lane;
                 int j = 0, cell = 0;
                 const bool hit = p < P && pairCell(gs, gr, p, j, cell);
-                const U32 peers = __match_any_sync(0xFFFFFFFFu, hit ? (U32)cell : 0x10000u + (U32)lane);
+                const U32 peers = __match_any_sync(0xFFFFFFFFu, hit ? (U32)cell : 0x80000000u + (U32)lane);
                 if (hit) {
                     const S64 idx = (S64)run[cell] + __popc(peers & ltMask);
                     if (idx < d.maxTileEntries) d.tileList[idx] = gs.entry[j];
@@ -675,19 +690,26 @@ cudaError_t launchBinning(const DrawDev& d, int maxBins, int numSMs, cudaStream_
         return n > 0 ? n : 1;
     });
     const int walkGrid = (int)min((S64)numSMs * walkCtas, (S64)(dl.totalChunks + kWalkWarps - 1) / kWalkWarps);
-    if (dl.totalChunks > 0) binCountKernel<<<walkGrid, kWalkThreads, walkSmem, stream>>>(dl);
-    binScanKernel<<<dl.totalBins, kBinThreads, 0, stream>>>(dl);
-    if (dl.totalChunks > 0) binScatterKernel<<<walkGrid, kWalkThreads, walkSmem, stream>>>(dl);
-    if (evCoarse) cudaEventRecord(evCoarse, stream);
+    cudaError_t e = cudaSuccess;
+    if (dl.totalChunks > 0) e = launchKernel(binCountKernel, walkGrid, kWalkThreads, walkSmem, stream, true, dl);
+    if (e == cudaSuccess) e = launchKernel(binScanKernel, dl.totalBins, kBinThreads, 0, stream, true, dl);
+    if (e == cudaSuccess && dl.totalChunks > 0)
+        e = launchKernel(binScatterKernel, walkGrid, kWalkThreads, walkSmem, stream, true, dl);
+    if (e == cudaSuccess && evCoarse) e = cudaEventRecord(evCoarse, stream);
+    if (e != cudaSuccess) return e;
     // Persistent coarse warps: as many CTAs as are resident at once, and no
     // more than the draw's units can keep busy.
     const S64 unitCtas = (dl.maxUnits + kCoarseWarps - 1) / kCoarseWarps;
     const int countGrid = (int)min((S64)numSMs * countCtas, unitCtas);
     const int scatterGrid = (int)min((S64)numSMs * scatterCtas, unitCtas);
-    coarseCountKernel<<<countGrid, kCoarseThreads, coarseCountSmem(dl.binLog2), stream>>>(dl);
-    coarseScanKernel<<<dl.totalBins, kBinThreads, sizeof(S32) * kBinWarps * ((size_t)1 << (2 * dl.binLog2)), stream>>>(dl);
-    coarseScatterKernel<<<scatterGrid, kCoarseThreads, coarseScatterSmem(dl.binLog2), stream>>>(dl);
-    return cudaGetLastError();
+    e = launchKernel(coarseCountKernel, countGrid, kCoarseThreads, coarseCountSmem(dl.binLog2), stream, true, dl);
+    if (e == cudaSuccess)
+        e = launchKernel(coarseScanKernel, dl.totalBins, kBinThreads,
+                         sizeof(S32) * kBinWarps * ((size_t)1 << (2 * dl.binLog2)), stream, true, dl);
+    if (e == cudaSuccess)
+        e = launchKernel(coarseScatterKernel, scatterGrid, kCoarseThreads, coarseScatterSmem(dl.binLog2), stream, true,
+                         dl);
+    return e;
 }
 
 }  // namespace cr

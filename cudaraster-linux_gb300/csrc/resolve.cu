@@ -11,6 +11,7 @@
 #include <cstdint>
 
 #include "cudaraster.h"
+#include "cudaraster/detail/launch.h"
 
 namespace cr {
 namespace {
@@ -58,11 +59,13 @@ extern "C" cr_status cr_resolve_color(const void* color, int32_t width, int32_t 
     const uint32_t* c = (const uint32_t*)color;
     uint32_t* o = (uint32_t*)out;
     const cudaStream_t s = (cudaStream_t)stream;
+    const int32_t ow = (int32_t)(out_row_bytes / 4);
+    cudaError_t e;
     switch (log2) {
-    case 0: cr::resolveKernel<0><<<grid, block, 0, s>>>(c, width, height, rowWords, o, out_row_bytes / 4); break;
-    case 1: cr::resolveKernel<1><<<grid, block, 0, s>>>(c, width, height, rowWords, o, out_row_bytes / 4); break;
-    case 2: cr::resolveKernel<2><<<grid, block, 0, s>>>(c, width, height, rowWords, o, out_row_bytes / 4); break;
-    default: cr::resolveKernel<3><<<grid, block, 0, s>>>(c, width, height, rowWords, o, out_row_bytes / 4); break;
+    case 0: e = cr::launchKernel(cr::resolveKernel<0>, grid, block, 0, s, false, c, width, height, rowWords, o, ow); break;
+    case 1: e = cr::launchKernel(cr::resolveKernel<1>, grid, block, 0, s, false, c, width, height, rowWords, o, ow); break;
+    case 2: e = cr::launchKernel(cr::resolveKernel<2>, grid, block, 0, s, false, c, width, height, rowWords, o, ow); break;
+    default: e = cr::launchKernel(cr::resolveKernel<3>, grid, block, 0, s, false, c, width, height, rowWords, o, ow); break;
     }
-    return cudaGetLastError() == cudaSuccess ? CR_OK : CR_ERR_CUDA;
+    return e == cudaSuccess ? CR_OK : CR_ERR_CUDA;
 }

@@ -12,6 +12,7 @@
 #include "cudaraster/detail/pipe_registry.h"
 
 #include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -122,8 +123,10 @@ struct cr_context {
     // Device memory.
     DevBuf triSubtris, triHeader, triData, chunkBinCount, chunkBinOffset, binCount, binStart, binUnitFirst, binList;
     DevBuf unitTileCount, tileCount, tileStart, tileList;
-    DevBuf instBuf;   // instance descriptors, then the prefix arrays (one copy per draw)
-    DevBuf counters;  // Counters, then one fine-stage tile counter per pipe group (one memset per draw)
+    // Per-draw block, written by one copy per draw: the zeroed Counters and one
+    // fine-stage tile counter per pipe group, then the instance descriptors
+    // and the prefix arrays.
+    DevBuf drawBlock;
     // Pinned staging.
     // Descriptor staging for asynchronous draws: a ring of pinned slots, each
     // reused only after the copy that read it has run (stageDone), so a host
@@ -136,7 +139,9 @@ struct cr_context {
     int stageNext = 0;
     Counters* hostCounters = nullptr;
     cudaEvent_t ev[5] = {};
-    bool eventsRecorded = false;
+    bool stageTiming = true;      // record the per-stage events of getStats
+    bool eventsRecorded = false;  // the last draw recorded them
+    bool drawn = false;           // a draw was enqueued (its counters are copied to hostCounters)
     int numSMs = 0;
     int device = 0;
     // Last draw.
@@ -260,8 +265,7 @@ cr_status cr_destroy(cr_context* ctx) {
     DevBuf* bufs[] = {&ctx->triSubtris, &ctx->triHeader, &ctx->triData, &ctx->chunkBinCount, &ctx->chunkBinOffset,
                       &ctx->binCount,
                       &ctx->binStart, &ctx->binUnitFirst, &ctx->binList, &ctx->unitTileCount,
-                      &ctx->tileCount, &ctx->tileStart, &ctx->tileList, &ctx->instBuf,
-                      &ctx->counters};
+                      &ctx->tileCount, &ctx->tileStart, &ctx->tileList, &ctx->drawBlock};
     for (DevBuf* b : bufs) b->release();
     for (int i = 0; i < cr_context::kStageSlots; i++) {
         if (ctx->hostStage[i]) cudaFreeHost(ctx->hostStage[i]);
@@ -449,6 +453,12 @@ cr_status cr_set_debug_params(cr_context* ctx, const cr_debug_params* p) {
     return CR_OK;
 }
 
+cr_status cr_set_stage_timing(cr_context* ctx, int32_t enabled) {
+    if (!ctx) return CR_ERR_INVALID_ARGUMENT;
+    ctx->stageTiming = enabled != 0;
+    return CR_OK;
+}
+
 cr_status cr_set_capacity(cr_context* ctx, int64_t ms, int64_t mb, int64_t mt) {
     if (!ctx) return CR_ERR_INVALID_ARGUMENT;
     if (ms < 0 || mb < 0 || mt < 0) return CR_ERR_INVALID_ARGUMENT;
@@ -463,6 +473,10 @@ cr_status cr_set_capacity(cr_context* ctx, int64_t ms, int64_t mb, int64_t mt) {
 
 // ------------------------------------------------------------------ drawing
 namespace {
+
+// Prefix arrays staged behind the instance descriptors, numInstances + 1
+// entries each: triangles (8 bytes), chunks, bins, tiles.
+constexpr size_t kPrefixBytesPerInstance = 8 + 3 * 4;
 
 struct Plan {
     std::vector<HostInstance> inst;
@@ -572,6 +586,16 @@ cr_status buildPlan(cr_context* ctx, const std::vector<HostInstance>& in, Plan& 
     return CR_OK;
 }
 
+// Bytes of the per-draw block: the counters (256-byte aligned), then the
+// instance descriptors and the prefix arrays.
+size_t counterBytes(const Plan& plan) {
+    return (sizeof(Counters) + sizeof(int32_t) * std::max<size_t>(plan.groups.size(), 1) + 255) & ~(size_t)255;
+}
+size_t drawBlockBytes(const Plan& plan) {
+    return counterBytes(plan) + sizeof(InstanceDev) * plan.inst.size() +
+           kPrefixBytesPerInstance * (plan.inst.size() + 1) + 64;
+}
+
 cr_status ensureCapacity(cr_context* ctx, const Plan& plan) {
     int64_t T = plan.totalTris;
     // Initial sizes in the spirit of CudaRaster.cpp:263-275 (subtriangle
@@ -602,12 +626,8 @@ cr_status ensureCapacity(cr_context* ctx, const Plan& plan) {
     CR_CUDA(ctx->tileCount.ensure((size_t)plan.totalTiles * 4), "cudaMalloc");
     CR_CUDA(ctx->tileStart.ensure((size_t)plan.totalTiles * 4), "cudaMalloc");
     CR_CUDA(ctx->tileList.ensure((size_t)ctx->maxTileEntries * 4), "cudaMalloc");
-    CR_CUDA(ctx->counters.ensure(sizeof(Counters) + sizeof(int32_t) * std::max<size_t>(plan.groups.size(), 1)),
-            "cudaMalloc");
-    size_t instBytes = sizeof(InstanceDev) * plan.inst.size();
-    size_t prefBytes = 4 * 3 * (plan.inst.size() + 1) + 8 * (plan.inst.size() + 1) + 64;
-    CR_CUDA(ctx->instBuf.ensure(instBytes + prefBytes), "cudaMalloc");
-    size_t stage = instBytes + prefBytes;
+    const size_t stage = drawBlockBytes(plan);
+    CR_CUDA(ctx->drawBlock.ensure(stage), "cudaMalloc");
     if (stage > ctx->hostStageBytes) {
         for (int i = 0; i < cr_context::kStageSlots; i++) {
             if (ctx->stageUsed[i]) CR_CUDA(cudaEventSynchronize(ctx->stageDone[i]), "cudaEventSynchronize");
@@ -628,7 +648,8 @@ cr_status ensureCapacity(cr_context* ctx, const Plan& plan) {
 
 DrawDev makeDrawDev(cr_context* ctx, const Plan& plan) {
     DrawDev d{};
-    d.inst = ctx->instBuf.as<InstanceDev>();
+    const size_t cb = counterBytes(plan);
+    d.inst = (const InstanceDev*)(ctx->drawBlock.as<char>() + cb);
     d.numInstances = (int)plan.inst.size();
     d.binLog2 = plan.binLog2;
     d.totalBins = plan.totalBins;
@@ -659,18 +680,20 @@ DrawDev makeDrawDev(cr_context* ctx, const Plan& plan) {
     d.tileStart = ctx->tileStart.as<int32_t>();
     d.tileList = ctx->tileList.as<uint32_t>();
     d.maxTileEntries = ctx->maxTileEntries;
-    char* pref = ctx->instBuf.as<char>() + sizeof(InstanceDev) * plan.inst.size();
+    char* pref = ctx->drawBlock.as<char>() + cb + sizeof(InstanceDev) * plan.inst.size();
     size_t n1 = plan.inst.size() + 1;
     d.triPrefix = (const int64_t*)pref;
     d.chunkPrefix = (const int32_t*)(pref + 8 * n1);
     d.binPrefix = d.chunkPrefix + n1;
     d.tilePrefix = d.binPrefix + n1;
-    d.counters = ctx->counters.as<Counters>();
-    d.fineTileCounter = (int32_t*)(ctx->counters.as<char>() + sizeof(Counters));
+    d.counters = ctx->drawBlock.as<Counters>();
+    d.fineTileCounter = (int32_t*)(ctx->drawBlock.as<char>() + sizeof(Counters));
     return d;
 }
 
 static_assert(sizeof(InstanceDev) % 8 == 0, "the prefix arrays follow the descriptors with 8-byte alignment");
+static_assert(offsetof(Counters, coarseWork) == 6 * sizeof(int32_t) && sizeof(Counters) >= 8 * sizeof(int32_t),
+              "cr_queue_counts exports the first 8 words of Counters");
 
 // Enqueues one draw of `plan` on `stream`. `stage` is pinned host memory for
 // the descriptors (the copy node reads it when a captured graph replays) and
@@ -679,20 +702,22 @@ static_assert(sizeof(InstanceDev) % 8 == 0, "the prefix arrays follow the descri
 cr_status launchDrawWith(cr_context* ctx, const Plan& plan, cudaStream_t stream, void* stage, Counters* hostCounters,
                          bool events) {
     DrawDev d = makeDrawDev(ctx, plan);
-    // Stage the descriptors through pinned memory.
+    // Stage the zeroed counters and the descriptors through pinned memory:
+    // one copy per draw.
     size_t n1 = plan.inst.size() + 1;
     size_t instBytes = sizeof(InstanceDev) * plan.inst.size();
-    char* hs = (char*)stage;
+    const size_t cb = counterBytes(plan);
+    memset(stage, 0, cb);
+    char* hs = (char*)stage + cb;
     for (size_t i = 0; i < plan.inst.size(); i++) memcpy(hs + i * sizeof(InstanceDev), &plan.inst[i].dev, sizeof(InstanceDev));
     char* hp = hs + instBytes;
     memcpy(hp, plan.triPrefix.data(), 8 * n1);
     memcpy(hp + 8 * n1, plan.chunkPrefix.data(), 4 * n1);
     memcpy(hp + 12 * n1, plan.binPrefix.data(), 4 * n1);
     memcpy(hp + 16 * n1, plan.tilePrefix.data(), 4 * n1);
-    CR_CUDA(cudaMemcpyAsync(ctx->instBuf.ptr, hs, instBytes + 20 * n1, cudaMemcpyHostToDevice, stream),
+    CR_CUDA(cudaMemcpyAsync(ctx->drawBlock.ptr, stage, cb + instBytes + kPrefixBytesPerInstance * n1,
+                            cudaMemcpyHostToDevice, stream),
             "cudaMemcpyAsync");
-    CR_CUDA(cudaMemsetAsync(ctx->counters.ptr, 0, sizeof(Counters) + sizeof(int32_t) * plan.groups.size(), stream),
-            "cudaMemsetAsync");
 
     if (events) CR_CUDA(cudaEventRecord(ctx->ev[0], stream), "cudaEventRecord");
     for (const Plan::Group& g : plan.groups)
@@ -706,11 +731,9 @@ cr_status launchDrawWith(cr_context* ctx, const Plan& plan, cudaStream_t stream,
         int ctas = ctx->tuning.fine_ctas_per_sm > 0 ? ctx->tuning.fine_ctas_per_sm : g.pipe->fineOccupancy(warps);
         CR_CUDA(g.pipe->launchFine(d, (int)gi, g.tileBegin, g.tileEnd, warps, ctas, ctx->numSMs, stream), "fine launch");
     }
-    if (events) {
-        CR_CUDA(cudaEventRecord(ctx->ev[4], stream), "cudaEventRecord");
-        ctx->eventsRecorded = true;
-    }
-    CR_CUDA(cudaMemcpyAsync(hostCounters, ctx->counters.ptr, sizeof(Counters), cudaMemcpyDeviceToHost, stream),
+    if (events) CR_CUDA(cudaEventRecord(ctx->ev[4], stream), "cudaEventRecord");
+    ctx->eventsRecorded = events;
+    CR_CUDA(cudaMemcpyAsync(hostCounters, ctx->drawBlock.ptr, sizeof(Counters), cudaMemcpyDeviceToHost, stream),
             "cudaMemcpyAsync");
     return CR_OK;
 }
@@ -719,8 +742,9 @@ cr_status launchDraw(cr_context* ctx, const Plan& plan, cudaStream_t stream) {
     const int slot = ctx->stageNext;
     ctx->stageNext = (slot + 1) % cr_context::kStageSlots;
     if (ctx->stageUsed[slot]) CR_CUDA(cudaEventSynchronize(ctx->stageDone[slot]), "cudaEventSynchronize");
-    cr_status st = launchDrawWith(ctx, plan, stream, ctx->hostStage[slot], ctx->hostCounters, true);
+    cr_status st = launchDrawWith(ctx, plan, stream, ctx->hostStage[slot], ctx->hostCounters, ctx->stageTiming);
     if (st != CR_OK) return st;
+    ctx->drawn = true;
     CR_CUDA(cudaEventRecord(ctx->stageDone[slot], stream), "cudaEventRecord");
     ctx->stageUsed[slot] = true;
     return CR_OK;
@@ -891,7 +915,7 @@ cr_status cr_batch_graph_create(cr_context* ctx, const cr_instance* instances, i
     st = buildPlan(ctx, v, g->plan);
     if (st == CR_OK) st = ensureCapacity(ctx, g->plan);
     if (st != CR_OK) { delete g; return st; }
-    size_t stageBytes = sizeof(InstanceDev) * g->plan.inst.size() + 20 * (g->plan.inst.size() + 1) + 64;
+    size_t stageBytes = drawBlockBytes(g->plan);
     cudaError_t e = cudaMallocHost(&g->stage, stageBytes);
     if (e == cudaSuccess) e = cudaMallocHost(&g->counters, sizeof(Counters));
     if (e != cudaSuccess) {
@@ -993,7 +1017,7 @@ cr_status cr_get_queue_buffers(cr_context* ctx, const int32_t** bin_counts, cons
     if (ctx->lastLayout.num_bins == 0) return fail(ctx, CR_ERR_INVALID_STATE, "CudaRaster: no draw to take queue counts from");
     *bin_counts = ctx->binCount.as<int32_t>();
     *tile_counts = ctx->tileCount.as<int32_t>();
-    *counters = ctx->counters.as<int32_t>();
+    *counters = ctx->drawBlock.as<int32_t>();
     return CR_OK;
 }
 
@@ -1012,18 +1036,17 @@ cr_status cr_queue_counts(cr_context* ctx, int32_t* bin_counts, int32_t num_bins
     if (tile_counts)
         CR_CUDA(cudaMemcpyAsync(tile_counts, ctx->tileCount.ptr, (size_t)num_tiles * 4, cudaMemcpyDeviceToDevice, s),
                 "cudaMemcpyAsync");
-    if (counters)
-        CR_CUDA(cudaMemcpyAsync(counters, ctx->counters.ptr, sizeof(Counters), cudaMemcpyDeviceToDevice, s),
+    if (counters)   // the 8 counters the header documents (the first 8 words of Counters), no more
+        CR_CUDA(cudaMemcpyAsync(counters, ctx->drawBlock.ptr, 8 * sizeof(int32_t), cudaMemcpyDeviceToDevice, s),
                 "cudaMemcpyAsync");
     return CR_OK;
 }
 
 cr_status cr_get_counters(cr_context* ctx, cr_counters* out) {
     if (!ctx || !out) return CR_ERR_INVALID_ARGUMENT;
-    if (ctx->eventsRecorded) {
-        CR_CUDA(cudaEventSynchronize(ctx->ev[4]), "cudaEventSynchronize");
-        // The counters copy follows the last event on the same stream.
-        cudaDeviceSynchronize();
+    if (ctx->drawn) {
+        // The last draw's counters copy is enqueued on its stream.
+        CR_CUDA(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
         const Counters& c = *ctx->hostCounters;
         ctx->last.num_subtris = ctx->last.num_tris + c.extraSubtris;
         ctx->last.bin_entries = c.binEntries;

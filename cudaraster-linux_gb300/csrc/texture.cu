@@ -6,6 +6,7 @@
 #include "cudaraster.h"
 #include "cudaraster/ShaderMath.hpp"
 #include "cudaraster/detail/device.cuh"
+#include "cudaraster/detail/launch.h"
 
 namespace cr {
 
@@ -37,9 +38,10 @@ extern "C" cr_status cr_texture_sample(const uint32_t* atlas, int32_t atlas_widt
                                        const float* uv, float* out, int64_t n, void* stream) {
     if (!cr::validSample(atlas, atlas_width, atlas_height, uv, out, n)) return CR_ERR_INVALID_ARGUMENT;
     if (n == 0) return CR_OK;
-    cr::textureSampleKernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
-        FW::TextureAtlas{atlas, atlas_width, atlas_height}, (const float2*)uv, (float4*)out, n);
-    return cudaGetLastError() == cudaSuccess ? CR_OK : CR_ERR_CUDA;
+    const cudaError_t e = cr::launchKernel(cr::textureSampleKernel, (unsigned)((n + 255) / 256), 256, 0,
+                                           (cudaStream_t)stream, false, FW::TextureAtlas{atlas, atlas_width, atlas_height},
+                                           (const float2*)uv, (float4*)out, n);
+    return e == cudaSuccess ? CR_OK : CR_ERR_CUDA;
 }
 
 extern "C" cr_status cr_texture_sample_hw(const uint32_t* atlas, int32_t atlas_width, int32_t atlas_height,
@@ -67,8 +69,8 @@ extern "C" cr_status cr_texture_sample_hw(const uint32_t* atlas, int32_t atlas_w
         e = cudaCreateTextureObject(&tex, &res, &td, nullptr);
     }
     if (e == cudaSuccess) {
-        cr::textureSampleHwKernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(tex, (const float2*)uv, (float4*)out, n);
-        e = cudaGetLastError();
+        e = cr::launchKernel(cr::textureSampleHwKernel, (unsigned)((n + 255) / 256), 256, 0, s, false, tex,
+                             (const float2*)uv, (float4*)out, n);
     }
     const cudaError_t es = cudaStreamSynchronize(s);
     if (tex) cudaDestroyTextureObject(tex);

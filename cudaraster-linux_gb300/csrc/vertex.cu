@@ -9,6 +9,7 @@
 #include "cudaraster.h"
 #include "cudaraster/ShaderMath.hpp"
 #include "cudaraster/detail/device.cuh"
+#include "cudaraster/detail/launch.h"
 
 namespace cr {
 
@@ -54,9 +55,10 @@ extern "C" cr_status cr_vertex_shader_passthrough(const float* model, int32_t mo
     cr::Mvp m;
     for (int k = 0; k < 16; k++) m.m[k] = mvp_row_major[k];
     int64_t grid = (num_vertices + 255) / 256;
-    cr::vertexPassthroughKernel<<<(unsigned)grid, 256, 0, (cudaStream_t)stream>>>(
-        model, model_stride, colors, color_stride, (float4*)out_vertices, out_stride_bytes / 16, num_vertices, m);
-    return cudaGetLastError() == cudaSuccess ? CR_OK : CR_ERR_CUDA;
+    const cudaError_t e = cr::launchKernel(cr::vertexPassthroughKernel, (unsigned)grid, 256, 0, (cudaStream_t)stream,
+                                           false, model, model_stride, colors, color_stride, (float4*)out_vertices,
+                                           out_stride_bytes / 16, num_vertices, m);
+    return e == cudaSuccess ? CR_OK : CR_ERR_CUDA;
 }
 
 // ---------------------------------------------------------------------------
@@ -183,11 +185,12 @@ template <VertexKind K>
 static cr_status launchVertex(const void* in, int64_t n, const VertexConstants& c, const GouraudArgs& g, void* out,
                               cudaStream_t stream) {
     const unsigned grid = (unsigned)((n + 255) / 256);
+    cudaError_t e;
     if (K == VertexKind::TexPhong && ((uintptr_t)in & 15) == 0)
-        vertexKernelStaged<K><<<grid, 256, 0, stream>>>((const float4*)in, n, c, g, (float4*)out);
+        e = launchKernel(vertexKernelStaged<K>, grid, 256, 0, stream, false, (const float4*)in, n, c, g, (float4*)out);
     else
-        vertexKernel<K><<<grid, 256, 0, stream>>>((const float*)in, n, c, g, (float4*)out);
-    return cudaGetLastError() == cudaSuccess ? CR_OK : CR_ERR_CUDA;
+        e = launchKernel(vertexKernel<K>, grid, 256, 0, stream, false, (const float*)in, n, c, g, (float4*)out);
+    return e == cudaSuccess ? CR_OK : CR_ERR_CUDA;
 }
 
 // The exact power over arrays (for its tests): out[i] = x[i]^y[i].
@@ -239,6 +242,7 @@ extern "C" cr_status cr_vertex_shader_tex_phong(const void* in_vertices, int64_t
 extern "C" cr_status cr_pow_exact(const float* x, const float* y, float* out, int64_t n, void* stream) {
     if (!x || !y || !out || n < 0 || !cr::gridFits(n)) return CR_ERR_INVALID_ARGUMENT;
     if (n == 0) return CR_OK;
-    cr::powExactKernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(x, y, out, n);
-    return cudaGetLastError() == cudaSuccess ? CR_OK : CR_ERR_CUDA;
+    const cudaError_t e = cr::launchKernel(cr::powExactKernel, (unsigned)((n + 255) / 256), 256, 0,
+                                           (cudaStream_t)stream, false, x, y, out, n);
+    return e == cudaSuccess ? CR_OK : CR_ERR_CUDA;
 }

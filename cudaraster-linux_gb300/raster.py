@@ -246,6 +246,11 @@ class CudaRaster:
         t = _lib.Tuning(bin_log2, bin_chunk_tris, coarse_unit_entries, fine_warps, fine_ctas_per_sm, fine_self_pixels)
         self._check(self._lib.cr_set_tuning(self._ctx, C.byref(t)))
 
+    def setStageTiming(self, enabled: bool) -> None:
+        """Per-stage events for getStats (on by default); off lets the stages' launches overlap."""
+        self._need_init()
+        self._check(self._lib.cr_set_stage_timing(self._ctx, 1 if enabled else 0))
+
     def setCapacity(self, max_subtris=0, max_bin_entries=0, max_tile_entries=0):
         self._need_init()
         self._check(self._lib.cr_set_capacity(self._ctx, int(max_subtris), int(max_bin_entries),

@@ -199,6 +199,11 @@ cr_status cr_set_index_buffer(cr_context* ctx, const void* indices, int64_t offs
                               int32_t num_tris);
 cr_status cr_set_tuning(cr_context* ctx, const cr_tuning* tuning);
 cr_status cr_set_debug_params(cr_context* ctx, const cr_debug_params* params);
+/* Per-stage timing of getStats (CudaRaster.cpp:346-363): on by default, as in
+ * the reference, each draw records a CUDA event between its stages. Off, the
+ * stages launch back to back with no event between them, so each stage's
+ * launch overlaps the end of the previous one, and cr_get_stats reports zeros. */
+cr_status cr_set_stage_timing(cr_context* ctx, int32_t enabled);
 /* Queue capacities (elements) for the next draws. All zero keeps the
  * reference-style estimates (CudaRaster.cpp:263-275); otherwise the given
  * sizes are used as they are (a predictor's sizing) and, when a draw

@@ -35,8 +35,8 @@ struct PipeImpl {
         int64_t n = triEnd - triBegin;
         if (n <= 0) return cudaSuccess;
         unsigned grid = (unsigned)((n + 255) / 256);
-        setupKernel<S, F & (kRenderDepth | kRenderLerp)><<<grid, 256, 0, stream>>>(d, instBegin, instEnd, triBegin, triEnd);
-        return cudaGetLastError();
+        return launchKernel(setupKernel<S, F & (kRenderDepth | kRenderLerp)>, grid, 256, 0, stream, true, d, instBegin,
+                            instEnd, (S64)triBegin, (S64)triEnd);
     }
     static size_t smemBytes(int warps) { return sizeof(typename FineTraits<FS, BS, S, F>::Smem) * (size_t)warps; }
     static cudaError_t launchFine(const DrawDev& d, int group, int32_t tileBegin, int32_t tileEnd, int warps,
@@ -49,8 +49,8 @@ struct PipeImpl {
         int64_t maxGrid = (warpsNeeded + warps - 1) / warps;
         if (grid > maxGrid) grid = maxGrid;
         if (grid < 1) grid = 1;
-        kern<<<(unsigned)grid, warps * 32, smemBytes(warps), stream>>>(d, group, tileBegin, tileEnd);
-        return cudaGetLastError();
+        return launchKernel(kern, (unsigned)grid, warps * 32, smemBytes(warps), stream, true, d, group, tileBegin,
+                            tileEnd);
     }
     // The fine kernel's shared-memory limit, set once on each device used.
     static void configureFine() {

@@ -37,6 +37,7 @@
 
 #include "../PixelPipe.hpp"
 #include "device.cuh"
+#include "launch.h"
 
 #include <type_traits>
 
@@ -257,6 +258,8 @@ __device__ __forceinline__ void fineTiles(const DrawDev& d, int group, S32 tileB
     typename Traits::Smem& sm = reinterpret_cast<typename Traits::Smem*>(fineSmemRaw)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     const U32 ltMask = (1u << lane) - 1u;
+    pdlWait();
+    pdlTrigger();
     if (__ldg(&d.counters->overflow)) return;
     const S32 selfPixels = d.fineSelfPixels > 0 ? d.fineSelfPixels : fineSelfPixelsDefault(S, kVisibility);
 

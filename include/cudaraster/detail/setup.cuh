@@ -10,6 +10,7 @@
 #pragma once
 
 #include "device.cuh"
+#include "launch.h"
 
 namespace cr {
 
@@ -220,6 +221,8 @@ __device__ __forceinline__ void fetchClip(const DrawDev& d, const float4* verts,
 // one pipe group [triBegin, triEnd) (global triangle slots).
 template <int S, U32 F>
 __global__ void __launch_bounds__(256, CR_SETUP_MIN_BLOCKS) setupKernel(DrawDev d, int instBegin, int instEnd, S64 triBegin, S64 triEnd) {
+    pdlWait();
+    pdlTrigger();
     S64 gt = triBegin + (S64)blockIdx.x * 256 + threadIdx.x;
     if (gt >= triEnd) return;
     int ii = instBegin + findInstance64(d.triPrefix + instBegin, instEnd - instBegin, gt);
