@@ -139,6 +139,7 @@ _SIGNATURES = {
     "cr_predictor_train_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
                                           C.c_float, C.c_float, C.c_float, C.c_float, C.c_void_p, C.c_void_p]),
     "cr_predictor_bad_rows": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_int32]),
+    "cr_predictor_set_loss_weights": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int64]),
     "cr_predictor_frame": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(QueueLayout),
                                      C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.POINTER(C.c_float), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -26,6 +26,8 @@
 #include <new>
 
 #include "cudaraster.h"
+#include "cudaraster/detail/launch.h"
+#include "cudaraster/detail/per_device.h"
 
 namespace cr {
 namespace predictor {
@@ -172,6 +174,255 @@ __global__ void adamKernel(float* __restrict__ w, __nv_bfloat16* __restrict__ w1
 __global__ void roundBf16Kernel(const float* __restrict__ w, __nv_bfloat16* __restrict__ w16, long long n) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) w16[i] = __float2bfloat16_rn(w[i]);
+}
+
+// ------------------------------------------------------ fused training step
+// One training step (or one gradient evaluation) in four launches instead of
+// a gather, six GEMMs, three bias reductions, the loss and Adam:
+//   F  (one CTA): gathers the batch and runs both hidden layers (z1, a1, z2,
+//      a2 into global memory);
+//   A  (one CTA per 32 outputs): its slice of the output layer, the weighted
+//      squared error and dY, the gradient of its rows of W3 / b3 (and their
+//      Adam update), and its part of dL/da2 = dY . W3 over its rows;
+//   B  (one CTA): dL/da2 summed over the A CTAs in CTA order, dz2,
+//      da1 = dz2 . W2, dz1, and the loss;
+//   C  (one thread per parameter of the hidden layers): the gradients of W1,
+//      b1, W2, b2 (and their Adam update).
+// No launch reads a parameter that another CTA of the same launch updates:
+// W3 rows are read only by the CTA that owns them, W2 is read by B and
+// updated by C, W1 and the hidden biases are read by F only. Every sum runs
+// in a fixed order, so results do not depend on timing. Sizes: inputs <=
+// kFusedMaxIn, hidden layers <= kFusedMaxHidden, batch <= kFusedMaxBatch.
+constexpr int kFusedMaxIn = 320;
+constexpr int kFusedMaxHidden = 64;
+constexpr int kFusedMaxBatch = 64;
+constexpr int kFusedOutSlice = 32;
+constexpr int kFusedThreads = 256;
+
+struct FusedNet {
+    int in, h1, h2, out, batch;
+    long long oW1, ob1, oW2, ob2, oW3, ob3;
+    const __nv_bfloat16* w16;       // parameters used (BF16)
+    __nv_bfloat16* w16Out;          // the same array, written by the Adam updates
+    float* master;                  // FP32 parameters (Adam master copy)
+    float* grad;                    // gradients [numParams]
+    float* adamM;
+    float* adamV;
+    int adam;                       // 0: gradients only
+    float lr, b1, b2, eps, c1, c2;
+    const float* xPool;
+    const float* tPool;
+    int poolRows;
+    const int32_t* rows;            // or NULL: rows 0..batch-1
+    const float* outWeights;        // per-output loss weights, or NULL (all 1)
+    float lossScale;                // 1 / (batch * sum of the output weights)
+    float* x;                       // [batch][in] gathered inputs
+    float* z1;                      // [batch][h1]
+    float* a1;
+    float* z2;                      // [batch][h2]
+    float* a2;
+    float* dz1;
+    float* dz2;
+    float* da2Part;                 // [numOutSlices][batch][h2]
+    float* lossPart;                // [numOutSlices]
+    float* loss;
+    int* badRows;
+};
+
+__device__ __forceinline__ void adamUpdate(const FusedNet& n, long long i, float g) {
+    n.grad[i] = g;
+    if (!n.adam) return;
+    const float mi = n.b1 * n.adamM[i] + (1.0f - n.b1) * g;
+    const float vi = n.b2 * n.adamV[i] + (1.0f - n.b2) * g * g;
+    n.adamM[i] = mi;
+    n.adamV[i] = vi;
+    const float wi = n.master[i] - n.lr * (mi / n.c1) / (sqrtf(vi / n.c2) + n.eps);
+    n.master[i] = wi;
+    n.w16Out[i] = __float2bfloat16_rn(wi);
+}
+
+// Pool row of batch row b; a row outside the pool reads row 0.
+__device__ __forceinline__ long long poolRow(const FusedNet& n, int b) {
+    const long long r = n.rows ? n.rows[b] : b;
+    return (r < 0 || r >= n.poolRows) ? 0 : r;
+}
+
+// Shared memory of kernel F: inputs, a1, W1 and W2 (BF16).
+__host__ __device__ constexpr size_t fusedSmemF(int in, int h1, int h2, int batch) {
+    return sizeof(float) * ((size_t)batch * in + (size_t)batch * h1) +
+           sizeof(__nv_bfloat16) * ((size_t)h1 * in + (size_t)h2 * h1);
+}
+// Shared memory of kernel A: a2, the dY slice, the W3 slice (BF16).
+__host__ __device__ constexpr size_t fusedSmemA(int h2, int batch) {
+    return sizeof(float) * ((size_t)batch * h2 + (size_t)batch * kFusedOutSlice) +
+           sizeof(__nv_bfloat16) * ((size_t)kFusedOutSlice * h2);
+}
+static_assert(fusedSmemF(kFusedMaxIn, kFusedMaxHidden, kFusedMaxHidden, kFusedMaxBatch) <= 227 * 1024,
+              "kernel F's shared memory must fit one CTA");
+static_assert(fusedSmemA(kFusedMaxHidden, kFusedMaxBatch) <= 48 * 1024, "kernel A needs no shared-memory opt-in");
+
+// Hidden layers of the batch, once; products accumulated in increasing k.
+__global__ void __launch_bounds__(1024) trainForwardKernel(FusedNet n) {
+    extern __shared__ __align__(16) unsigned char smemRaw[];
+    const int B = n.batch, IN = n.in, H1 = n.h1, H2 = n.h2;
+    float* xs = reinterpret_cast<float*>(smemRaw);
+    float* a1 = xs + (size_t)B * IN;
+    __nv_bfloat16* w1 = reinterpret_cast<__nv_bfloat16*>(a1 + (size_t)B * H1);
+    __nv_bfloat16* w2 = w1 + (size_t)H1 * IN;
+    pdlWait();
+    pdlTrigger();
+    const int t = threadIdx.x, nt = blockDim.x;
+    for (int i = t; i < B * IN; i += nt) {
+        const int b = i / IN, k = i - b * IN;
+        const long long r = n.rows ? n.rows[b] : b;
+        if ((r < 0 || r >= n.poolRows) && k == 0) atomicOr(n.badRows, 1);
+        const float v = n.xPool[poolRow(n, b) * IN + k];
+        xs[i] = v;
+        n.x[i] = v;
+    }
+    for (int i = t; i < H1 * IN; i += nt) w1[i] = n.w16[n.oW1 + i];
+    for (int i = t; i < H2 * H1; i += nt) w2[i] = n.w16[n.oW2 + i];
+    __syncthreads();
+    for (int i = t; i < B * H1; i += nt) {
+        const int b = i / H1, j = i - b * H1;
+        const float* xr = xs + (size_t)b * IN;
+        const __nv_bfloat16* wr = w1 + (size_t)j * IN;
+        float s = 0.0f;
+        for (int k = 0; k < IN; k++) s = fmaf(__bfloat162float(wr[k]), xr[k], s);
+        const float z = s + __bfloat162float(n.w16[n.ob1 + j]);
+        const float a = gelu(z);
+        a1[i] = a;
+        n.z1[i] = z;
+        n.a1[i] = a;
+    }
+    __syncthreads();
+    for (int i = t; i < B * H2; i += nt) {
+        const int b = i / H2, j = i - b * H2;
+        const float* ar = a1 + (size_t)b * H1;
+        const __nv_bfloat16* wr = w2 + (size_t)j * H1;
+        float s = 0.0f;
+        for (int k = 0; k < H1; k++) s = fmaf(__bfloat162float(wr[k]), ar[k], s);
+        const float z = s + __bfloat162float(n.w16[n.ob2 + j]);
+        n.z2[i] = z;
+        n.a2[i] = gelu(z);
+    }
+}
+
+__global__ void __launch_bounds__(kFusedThreads) trainOutputKernel(FusedNet n) {
+    extern __shared__ __align__(16) unsigned char smemRaw[];
+    __shared__ float red[kFusedThreads / 32];
+    const int B = n.batch, H2 = n.h2;
+    float* a2 = reinterpret_cast<float*>(smemRaw);
+    float* dy = a2 + (size_t)B * H2;                                                          // [B][slice]
+    __nv_bfloat16* w3 = reinterpret_cast<__nv_bfloat16*>(dy + (size_t)B * kFusedOutSlice);   // [slice][H2]
+    pdlWait();
+    pdlTrigger();
+    const int t = threadIdx.x, nt = blockDim.x;
+    const int o0 = blockIdx.x * kFusedOutSlice;
+    const int no = min(kFusedOutSlice, n.out - o0);
+    for (int i = t; i < B * H2; i += nt) a2[i] = n.a2[i];
+    for (int i = t; i < no * H2; i += nt) w3[i] = n.w16[n.oW3 + (long long)o0 * H2 + i];
+    __syncthreads();
+    // Output slice: y, the weighted error and dY = 2 w (y - t) * lossScale.
+    float l = 0.0f;
+    for (int i = t; i < B * kFusedOutSlice; i += nt) {
+        const int b = i / kFusedOutSlice, q = i - b * kFusedOutSlice;
+        float d = 0.0f;
+        if (q < no) {
+            const int o = o0 + q;
+            const float* ar = a2 + (size_t)b * H2;
+            const __nv_bfloat16* wr = w3 + (size_t)q * H2;
+            float s = 0.0f;
+            for (int k = 0; k < H2; k++) s = fmaf(__bfloat162float(wr[k]), ar[k], s);
+            const float y = s + __bfloat162float(n.w16[n.ob3 + o]);
+            const float e = y - n.tPool[poolRow(n, b) * n.out + o];
+            const float wo = n.outWeights ? n.outWeights[o] : 1.0f;
+            d = 2.0f * wo * e * n.lossScale;
+            l = fmaf(wo * e, e, l);
+        }
+        dy[i] = d;
+    }
+    // The slice's loss, summed in a fixed order.
+    for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xFFFFFFFFu, l, o);
+    if ((t & 31) == 0) red[t >> 5] = l;
+    __syncthreads();
+    if (t == 0) {
+        float sum = 0.0f;
+        for (int w = 0; w < nt / 32; w++) sum += red[w];
+        n.lossPart[blockIdx.x] = sum;
+    }
+    // dL/da2 over this slice's rows: part[b][j] = sum_q dY[b][q] W3[q][j].
+    for (int i = t; i < B * H2; i += nt) {
+        const int b = i / H2, j = i - b * H2;
+        float sum = 0.0f;
+        for (int q = 0; q < no; q++)
+            sum = fmaf(dy[b * kFusedOutSlice + q], __bfloat162float(w3[(size_t)q * H2 + j]), sum);
+        n.da2Part[(size_t)blockIdx.x * B * H2 + i] = sum;
+    }
+    // Gradients of the slice's rows of W3 and b3 (batch order), then Adam.
+    for (int i = t; i < no * (H2 + 1); i += nt) {
+        const int q = i / (H2 + 1), j = i - q * (H2 + 1);
+        float g = 0.0f;
+        if (j < H2) {
+            for (int b = 0; b < B; b++) g = fmaf(dy[b * kFusedOutSlice + q], a2[(size_t)b * H2 + j], g);
+            adamUpdate(n, n.oW3 + (long long)(o0 + q) * H2 + j, g);
+        } else {
+            for (int b = 0; b < B; b++) g += dy[b * kFusedOutSlice + q];
+            adamUpdate(n, n.ob3 + o0 + q, g);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(1024) trainHiddenKernel(FusedNet n, int slices) {
+    __shared__ float dz2s[kFusedMaxBatch * kFusedMaxHidden];
+    pdlWait();
+    pdlTrigger();
+    const int B = n.batch, H1 = n.h1, H2 = n.h2;
+    const int t = threadIdx.x, nt = blockDim.x;
+    for (int i = t; i < B * H2; i += nt) {
+        float sum = 0.0f;
+        for (int g = 0; g < slices; g++) sum += n.da2Part[(size_t)g * B * H2 + i];
+        const float d = sum * geluGrad(n.z2[i]);
+        dz2s[i] = d;
+        n.dz2[i] = d;
+    }
+    __syncthreads();
+    for (int i = t; i < B * H1; i += nt) {
+        const int b = i / H1, k = i - b * H1;
+        float sum = 0.0f;
+        for (int j = 0; j < H2; j++)
+            sum = fmaf(dz2s[b * H2 + j], __bfloat162float(n.w16[n.oW2 + (long long)j * H1 + k]), sum);
+        n.dz1[i] = sum * geluGrad(n.z1[i]);
+    }
+    if (t == 0) {
+        float sum = 0.0f;
+        for (int g = 0; g < slices; g++) sum += n.lossPart[g];
+        *n.loss = sum * n.lossScale;
+    }
+}
+
+// One thread per parameter of the hidden layers: W1, b1, W2, b2 in layout order.
+__global__ void __launch_bounds__(256) trainWeightsKernel(FusedNet n) {
+    pdlWait();
+    pdlTrigger();
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int B = n.batch, IN = n.in, H1 = n.h1, H2 = n.h2;
+    if (i >= n.oW3) return;
+    float g = 0.0f;
+    if (i < n.ob1) {
+        const int j = (int)(i / IN), k = (int)(i - (long long)j * IN);
+        for (int b = 0; b < B; b++) g = fmaf(n.dz1[b * H1 + j], n.x[(size_t)b * IN + k], g);
+    } else if (i < n.oW2) {
+        const int j = (int)(i - n.ob1);
+        for (int b = 0; b < B; b++) g += n.dz1[b * H1 + j];
+    } else if (i < n.ob2) {
+        const int j = (int)((i - n.oW2) / H1), k = (int)((i - n.oW2) - (long long)j * H1);
+        for (int b = 0; b < B; b++) g = fmaf(n.dz2[b * H2 + j], n.a1[b * H1 + k], g);
+    } else {
+        const int j = (int)(i - n.ob2);
+        for (int b = 0; b < B; b++) g += n.dz2[b * H2 + j];
+    }
+    adamUpdate(n, i, g);
 }
 
 // ---------------------------------------------------------------- features
@@ -437,12 +688,21 @@ struct cr_predictor {
     float *x = nullptr, *t = nullptr, *z1 = nullptr, *a1 = nullptr, *z2 = nullptr, *a2 = nullptr, *y = nullptr;
     float *dy = nullptr, *dz2 = nullptr, *dz1 = nullptr, *loss = nullptr;
     int* badRows = nullptr;         // set when a batch named a row outside its pool
+    // Fused training step (sizes within the kFused* limits).
+    bool fused = false;
+    int slices = 0;                 // output slices of kFusedOutSlice rows
+    float* da2Part = nullptr;       // [slices][maxBatch][h2]
+    float* lossPart = nullptr;      // [slices]
+    float* outWeights = nullptr;    // per-output loss weights (NULL: all 1)
+    double sumWeights = 0.0;
 };
 
 namespace {
 
 void freePredictor(cr_predictor* p) {
     if (!p) return;
+    cudaFree(p->da2Part);
+    cudaFree(p->outWeights);
     cudaFree(p->master);
     cudaFree(p->w16);
     cudaFree(p->grad);
@@ -480,6 +740,68 @@ void backward(cr_predictor* p, int batch, cudaStream_t s) {
                                              p->h1, nullptr, p->z1, p->h1);
     gemm<float, float, kEpiPlain>(s, p->h1, p->in, batch, p->dz1, 1, p->h1, p->x, p->in, 1, g + p->oW1, p->in);
     colSumKernel<<<(p->h1 + 255) / 256, 256, 0, s>>>(p->dz1, batch, p->h1, p->h1, g + p->ob1);
+}
+
+// The fused step: gradients of `batch` rows into p->grad and the loss into
+// p->loss, and with adam the Adam update of every parameter (p->step already
+// advanced).
+cr_status trainFused(cr_predictor* p, const float* xPool, const float* tPool, int poolRows, const int32_t* rows,
+                     int batch, bool adam, float lr, float beta1, float beta2, float eps, cudaStream_t s) {
+    FusedNet n;
+    memset(&n, 0, sizeof(n));
+    n.in = p->in;
+    n.h1 = p->h1;
+    n.h2 = p->h2;
+    n.out = p->out;
+    n.batch = batch;
+    n.oW1 = p->oW1;
+    n.ob1 = p->ob1;
+    n.oW2 = p->oW2;
+    n.ob2 = p->ob2;
+    n.oW3 = p->oW3;
+    n.ob3 = p->ob3;
+    n.w16 = p->w16;
+    n.w16Out = p->w16;
+    n.master = p->master;
+    n.grad = p->grad;
+    n.adamM = p->adamM;
+    n.adamV = p->adamV;
+    n.adam = adam ? 1 : 0;
+    n.lr = lr;
+    n.b1 = beta1;
+    n.b2 = beta2;
+    n.eps = eps;
+    n.c1 = adam ? (float)(1.0 - std::pow((double)beta1, (double)p->step)) : 1.0f;
+    n.c2 = adam ? (float)(1.0 - std::pow((double)beta2, (double)p->step)) : 1.0f;
+    n.xPool = xPool;
+    n.tPool = tPool;
+    n.poolRows = poolRows;
+    n.rows = rows;
+    n.outWeights = p->outWeights;
+    n.lossScale = (float)(1.0 / ((double)batch * (p->outWeights ? p->sumWeights : (double)p->out)));
+    n.x = p->x;
+    n.z1 = p->z1;
+    n.a1 = p->a1;
+    n.z2 = p->z2;
+    n.a2 = p->a2;
+    n.dz1 = p->dz1;
+    n.dz2 = p->dz2;
+    n.da2Part = p->da2Part;
+    n.lossPart = p->lossPart;
+    n.loss = p->loss;
+    n.badRows = p->badRows;
+    static cr::OncePerDevice attribute;
+    attribute.run([] {
+        cudaFuncSetAttribute(trainForwardKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)fusedSmemF(kFusedMaxIn, kFusedMaxHidden, kFusedMaxHidden, kFusedMaxBatch));
+    });
+    cudaError_t e = cr::launchKernel(trainForwardKernel, 1, 1024, fusedSmemF(n.in, n.h1, n.h2, batch), s, false, n);
+    if (e == cudaSuccess)
+        e = cr::launchKernel(trainOutputKernel, p->slices, kFusedThreads, fusedSmemA(n.h2, batch), s, true, n);
+    if (e == cudaSuccess) e = cr::launchKernel(trainHiddenKernel, 1, 1024, 0, s, true, n, p->slices);
+    if (e == cudaSuccess)
+        e = cr::launchKernel(trainWeightsKernel, (unsigned)((p->oW3 + 255) / 256), 256, 0, s, true, n);
+    return e == cudaSuccess ? CR_OK : CR_ERR_CUDA;
 }
 
 cr_status gatherBatch(cr_predictor* p, const float* xPool, const float* tPool, int poolRows, const int32_t* rows,
@@ -536,6 +858,17 @@ cr_status cr_predictor_create(cr_predictor** out, int32_t inputs, int32_t hidden
     if (e != cudaSuccess) {
         freePredictor(p);
         return e == cudaErrorMemoryAllocation ? CR_ERR_OUT_OF_MEMORY : CR_ERR_CUDA;
+    }
+    p->fused = inputs <= kFusedMaxIn && hidden1 <= kFusedMaxHidden && hidden2 <= kFusedMaxHidden &&
+               max_batch <= kFusedMaxBatch;
+    if (p->fused) {
+        p->slices = (outputs + kFusedOutSlice - 1) / kFusedOutSlice;
+        e = cudaMalloc(&p->da2Part, ((size_t)p->slices * max_batch * hidden2 + p->slices) * sizeof(float));
+        if (e != cudaSuccess) {
+            freePredictor(p);
+            return e == cudaErrorMemoryAllocation ? CR_ERR_OUT_OF_MEMORY : CR_ERR_CUDA;
+        }
+        p->lossPart = p->da2Part + (size_t)p->slices * max_batch * hidden2;
     }
     float* a = p->act;
     p->x = a;   a += B * inputs;
@@ -600,10 +933,16 @@ cr_status cr_predictor_gradients(cr_predictor* p, const float* x_pool, const flo
         (!rows && batch > pool_rows))
         return CR_ERR_INVALID_ARGUMENT;
     cudaStream_t s = (cudaStream_t)stream;
-    if (gatherBatch(p, x_pool, target_pool, pool_rows, rows, batch, s) != CR_OK) return CR_ERR_CUDA;
-    forward(p, batch, s);
-    mseKernel<<<1, 1024, 0, s>>>(p->y, p->t, batch * p->out, p->dy, p->loss);
-    backward(p, batch, s);
+    if (p->fused) {
+        if (trainFused(p, x_pool, target_pool, pool_rows, rows, batch, false, 0.0f, 0.0f, 0.0f, 1.0f, s) != CR_OK)
+            return CR_ERR_CUDA;
+    } else {
+        if (p->outWeights) return CR_ERR_UNSUPPORTED;
+        if (gatherBatch(p, x_pool, target_pool, pool_rows, rows, batch, s) != CR_OK) return CR_ERR_CUDA;
+        forward(p, batch, s);
+        mseKernel<<<1, 1024, 0, s>>>(p->y, p->t, batch * p->out, p->dy, p->loss);
+        backward(p, batch, s);
+    }
     cudaError_t e = cudaSuccess;
     if (grads) e = cudaMemcpyAsync(grads, p->grad, (size_t)p->numParams * sizeof(float), cudaMemcpyDeviceToDevice, s);
     if (e == cudaSuccess && loss) e = cudaMemcpyAsync(loss, p->loss, sizeof(float), cudaMemcpyDeviceToDevice, s);
@@ -616,6 +955,18 @@ cr_status cr_predictor_train_step(cr_predictor* p, const float* x_pool, const fl
                                   float* loss, void* stream) {
     if (!(lr >= 0.0f) || !(beta1 >= 0.0f && beta1 < 1.0f) || !(beta2 >= 0.0f && beta2 < 1.0f) || !(eps > 0.0f))
         return CR_ERR_INVALID_ARGUMENT;
+    if (p && p->fused) {
+        if (!x_pool || !target_pool || batch <= 0 || batch > p->maxBatch || pool_rows <= 0 ||
+            (!rows && batch > pool_rows))
+            return CR_ERR_INVALID_ARGUMENT;
+        p->step++;
+        cudaStream_t s = (cudaStream_t)stream;
+        if (trainFused(p, x_pool, target_pool, pool_rows, rows, batch, true, lr, beta1, beta2, eps, s) != CR_OK)
+            return CR_ERR_CUDA;
+        if (loss && cudaMemcpyAsync(loss, p->loss, sizeof(float), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+            return CR_ERR_CUDA;
+        return CR_OK;
+    }
     cr_status st = cr_predictor_gradients(p, x_pool, target_pool, pool_rows, rows, batch, nullptr, loss, stream);
     if (st != CR_OK) return st;
     p->step++;
@@ -628,6 +979,30 @@ cr_status cr_predictor_train_step(cr_predictor* p, const float* x_pool, const fl
 }
 
 int64_t cr_predictor_steps(const cr_predictor* p) { return p ? p->step : 0; }
+
+cr_status cr_predictor_set_loss_weights(cr_predictor* p, const float* host, int64_t n) {
+    if (!p) return CR_ERR_INVALID_ARGUMENT;
+    if (!host) {
+        cudaFree(p->outWeights);
+        p->outWeights = nullptr;
+        p->sumWeights = 0.0;
+        return CR_OK;
+    }
+    if (n != p->out) return CR_ERR_INVALID_ARGUMENT;
+    double sum = 0.0;
+    for (int64_t i = 0; i < n; i++) {
+        if (!(host[i] >= 0.0f) || !std::isfinite(host[i])) return CR_ERR_INVALID_ARGUMENT;
+        sum += host[i];
+    }
+    if (!(sum > 0.0)) return CR_ERR_INVALID_ARGUMENT;
+    if (!p->fused) return CR_ERR_UNSUPPORTED;
+    if (!p->outWeights && cudaMalloc(&p->outWeights, (size_t)n * sizeof(float)) != cudaSuccess)
+        return CR_ERR_OUT_OF_MEMORY;
+    if (cudaMemcpy(p->outWeights, host, (size_t)n * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+        return CR_ERR_CUDA;
+    p->sumWeights = sum;
+    return CR_OK;
+}
 
 cr_status cr_predictor_bad_rows(cr_predictor* p, int32_t* flag, int32_t reset) {
     if (!p || !flag) return CR_ERR_INVALID_ARGUMENT;

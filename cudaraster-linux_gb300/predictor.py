@@ -123,6 +123,14 @@ class Network:
                                                      batch, lr, betas[0], betas[1], eps, _p(self._loss), _s(stream)))
         return self._loss
 
+    def set_loss_weights(self, weights: np.ndarray | None) -> None:
+        """Per-output weights of the squared error (None: equal weights)."""
+        if weights is None:
+            _lib.check(self.lib.cr_predictor_set_loss_weights(self.handle, None, 0))
+            return
+        a = np.ascontiguousarray(weights, dtype=np.float32)
+        _lib.check(self.lib.cr_predictor_set_loss_weights(self.handle, a.ctypes.data_as(C.POINTER(C.c_float)), a.size))
+
     def bad_rows(self, reset: bool = True) -> bool:
         """True if a batch named a row outside its pool since the last reset."""
         f = C.c_int32()

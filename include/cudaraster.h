@@ -468,6 +468,13 @@ cr_status cr_predictor_frame(cr_predictor* p, const int32_t* bin_counts, const i
                              const float* logs_prev, float* logs_cur, const float* logs_target_base,
                              const float* logs_target_trend, float* target, const float* camera_delta_ahead,
                              float* x_next, float* per_bin, void* fetch, void* stream);
+/* Per-output loss weights w (outputs values >= 0, sum > 0; NULL restores
+ * equal weights): loss = sum_b sum_o w_o (y - t)^2 / (batch * sum_o w_o).
+ * Copied; synchronous. Available for networks within the fused training
+ * step's sizes (inputs <= 320, hidden layers <= 64, max_batch <= 64), which
+ * every gradient and training call of such a network uses: four launches
+ * per step. */
+cr_status cr_predictor_set_loss_weights(cr_predictor* p, const float* weights, int64_t n);
 /* *flag = nonzero if a batch since the last reset named a row outside its
  * pool; reset != 0 clears it. Synchronous. */
 cr_status cr_predictor_bad_rows(cr_predictor* p, int32_t* flag, int32_t reset);

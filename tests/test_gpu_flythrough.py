@@ -4,7 +4,8 @@ plain) every frame of the pipelined, predictor-sized path is bit-identical to
 the plain path, a frame matches the CPU oracle, and forced misses are caught
 by the overflow flags and redrawn exactly; over the whole 300-frame loop (the
 first 50 plain) the predictor sizes the queues more tightly than the
-previous-frame sizing of the reference."""
+previous-frame sizing of the reference. Whether the trained network also beats
+the trend extrapolation it starts from is recorded by an expected failure."""
 import math
 
 import numpy as np
@@ -77,16 +78,42 @@ def test_flythrough_frame_matches_oracle(fly, plain):
     assert_same(gc, gd, color, depth, f"fly-through frame {f}")
 
 
-def test_predictor_sizes_tighter_than_previous_frame_sizing(fly):
-    res = pkg_mod("workloads").run_flythrough_predicted(fly, LOOP, LOOP_TRAIN)
-    assert res["misses"] == [0, 0] or sum(res["misses"]) <= 2
+@pytest.fixture(scope="module")
+def loop(fly):
+    """The whole 300-frame loop, the first 50 frames plain, the rest predictor-sized."""
+    return pkg_mod("workloads").run_flythrough_predicted(fly, LOOP, LOOP_TRAIN)
+
+
+def _errors(loop):
+    """Mean absolute log error of the bin / tile totals sized two frames ahead, per
+    layer: the predictor, the reference's sizing from the last draw it has seen,
+    and trend extrapolation alone (what the network predicts untrained)."""
+    out = {}
     for k in range(2):
-        r = sorted((x for x in res["records"] if x["layer"] == k), key=lambda x: x["frame"])
+        r = sorted((x for x in loop["records"] if x["layer"] == k), key=lambda x: x["frame"])
         for q in ("bin", "tile"):
-            actual = np.array([x[q] for x in r])
-            pred = np.array([x["pred_" + q] for x in r])
-            # The reference sizes a draw from the last draw it has seen: two frames back here.
-            err_pred = np.abs(np.log(actual[2:] / pred[2:])).mean()
-            err_prev = np.abs(np.log(actual[2:] / actual[:-2])).mean()
-            assert err_pred < err_prev, (k, q, err_pred, err_prev)
-            assert math.isfinite(err_pred)
+            a = np.array([x[q] for x in r], np.float64)
+            p = np.array([x["pred_" + q] for x in r], np.float64)
+            tgt = a[3:]
+            out[(k, q)] = {"predictor": float(np.abs(np.log(tgt / p[3:])).mean()),
+                           "previous_frame": float(np.abs(np.log(tgt / a[1:-2])).mean()),
+                           "trend_only": float(np.abs(np.log(tgt / (a[1:-2] ** 3 / a[:-3] ** 2))).mean())}
+    return out
+
+
+def test_predictor_sizes_tighter_than_previous_frame_sizing(loop):
+    assert loop["misses"] == [0, 0] or sum(loop["misses"]) <= 2
+    for key, e in _errors(loop).items():
+        assert math.isfinite(e["predictor"])
+        assert e["predictor"] < e["previous_frame"], (key, e)
+
+
+@pytest.mark.xfail(reason="on this camera loop the trend's residual of the queue totals is not predictable from the "
+                          "network's inputs (pooled histogram, camera move): a least-squares fit on them removes "
+                          "about 2% of it even in sample, and the trained correction ties or loses to the trend",
+                   strict=False)
+def test_trained_beats_trend_only(loop):
+    errs = _errors(loop)
+    print({f"{k}/{q}": {n: round(v, 5) for n, v in e.items()} for (k, q), e in errs.items()})
+    for key, e in errs.items():
+        assert e["predictor"] < e["trend_only"], (key, e)

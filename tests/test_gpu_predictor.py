@@ -235,3 +235,48 @@ def test_fused_frame_step_matches_the_separate_kernels_and_oracle(cuda):
     c, pv = cur.cpu().numpy().astype(np.float64)[:n], logs[1].cpu().numpy().astype(np.float64)[:n]
     heads = np.expm1(c[-2:] + 2.0 * (c[-2:] - pv[-2:]) + y[-2:])
     np.testing.assert_allclose(fetch.cpu().numpy()[:2], heads, rtol=2e-4)
+
+
+def test_weighted_loss_gradients_match_oracle(cuda):
+    """Per-output loss weights (cr_predictor_set_loss_weights): loss and every
+    gradient against the oracle's weighted squared error; equal weights give
+    the unweighted loss back."""
+    net = _net(seed=13)
+    rng = np.random.default_rng(14)
+    x, t, xd, td = _pools(rng)
+    rows = np.array([1, 9, 33, 4, 4, 20], dtype=np.int32)
+    w = rng.uniform(0.0, 2.0, DIMS[3]).astype(np.float32)
+    w[-2:] = 50.0
+    net.set_loss_weights(w)
+    g, loss = net.gradients(xd, td, torch.from_numpy(rows).cuda())
+    ref_loss, ref_g = mo.loss_and_grad(net.get_params_bf16(), DIMS, x[rows], t[rows], weights=w)
+    assert float(loss.item()) == pytest.approx(ref_loss, rel=2e-5)
+    _check_grads(g.cpu().numpy(), ref_g)
+    net.set_loss_weights(None)
+    g2, loss2 = net.gradients(xd, td, torch.from_numpy(rows).cuda())
+    ref_loss2, ref_g2 = mo.loss_and_grad(net.get_params_bf16(), DIMS, x[rows], t[rows])
+    assert float(loss2.item()) == pytest.approx(ref_loss2, rel=2e-5)
+    _check_grads(g2.cpu().numpy(), ref_g2)
+
+
+def test_fused_training_step_time(cuda):
+    """One training step (gather, forward, loss, backward, Adam) of the queue
+    predictor's network at batch 32 is four launches and under 50 us."""
+    net = _net(seed=15, dims=(262, 64, 64, 1022))
+    rng = np.random.default_rng(16)
+    x = torch.from_numpy(rng.normal(0, 1, (64, 262)).astype(np.float32)).cuda()
+    t = torch.from_numpy(rng.normal(0, 0.5, (64, 1022)).astype(np.float32)).cuda()
+    rows = torch.arange(32, dtype=torch.int32, device="cuda")
+    for _ in range(5):
+        net.train_step(x, t, rows, 32)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n = 50
+    a.record()
+    for _ in range(n):
+        net.train_step(x, t, rows, 32)
+    b.record()
+    torch.cuda.synchronize()
+    us = a.elapsed_time(b) * 1e3 / n
+    print(f"fused training step: {us:.1f} us")
+    assert us < 50.0, us

@@ -144,3 +144,35 @@ def test_repeated_draws_are_identical(cuda, pipe):
     for _ in range(4):
         again = gpu_render(pipe, sc, clear, cr=cr)
         assert_same(again[0], again[1], first[0], first[1], f"{pipe} repeat")
+
+
+@pytest.mark.parametrize("pipe", ["PixelPipe_gouraud", "PixelPipe_gouraud_msaa4", "PixelPipe_gouraud_srcover"])
+def test_equal_depth_copies_keep_the_first(cuda, pipe):
+    """Every triangle drawn three times with the same positions (equal depths at
+    every sample) and different colours, the copies scattered through the
+    submission order: under depth LESS the first copy submitted keeps every
+    sample -- through the visibility keys of the depth-resolved pipes, whose
+    ties go to the lower list position, and through the ordered path."""
+    from conftest import pkg_mod
+    from helpers import PIPE_SAMPLES
+    base = pkg_mod("scenes").soup(3000, 256, 192, seed=51, median_px=10.0,
+                                  alpha_range=(0.2, 1.0) if "srcover" in pipe else None)
+    rng = np.random.default_rng(52)
+    T = base["indices"].shape[0]
+    verts = []
+    for _ in range(3):
+        v = base["vertices"].copy()
+        v[:, 4:8] = (np.round(rng.uniform(0, 1, (v.shape[0], 4)) * 255) / 255).astype(np.float32)
+        verts.append(v)
+    V = base["vertices"].shape[0]
+    allv = np.concatenate(verts)
+    tris = np.concatenate([base["indices"] + k * V for k in range(3)])
+    order = rng.permutation(3 * T)
+    sc = dict(base, vertices=allv, indices=np.ascontiguousarray(tris[order], dtype=np.int32))
+    sc["samples"] = PIPE_SAMPLES.get(pipe, 1)
+    p = pkg()
+    clear = (p.color_to_abgr(0.1, 0.1, 0.1, 1.0), p.clear_depth_from_float(1.0))
+    gc, gd, _, _ = gpu_render(pipe, sc, clear)
+    rc, rd, st = oracle_render(pipe, sc, clear)
+    assert st["zmin_violations"] == 0
+    assert_same(gc, gd, rc, rd, f"{pipe} equal-depth copies")
