@@ -247,138 +247,190 @@ __device__ __forceinline__ long long poolRow(const FusedNet& n, int b) {
     return (r < 0 || r >= n.poolRows) ? 0 : r;
 }
 
-// Shared memory of kernel F: inputs, a1, W1 and W2 (BF16).
+// Rows in shared memory are padded to a multiple of 8 elements (16 bytes of
+// BF16): 128-bit loads, and consecutive rows start on different banks.
+__host__ __device__ constexpr int padRow(int n) { return (n + 7) & ~7; }
+__host__ __device__ constexpr int padRowOdd(int n) { return padRow(n) + 8; }   // 16 bytes more: 4 banks apart
+
+// Shared memory of kernel F: inputs [B][padRow(in)], a1 [B][padRowOdd(h1)] (floats),
+// W1 [h1][padRow(in)] and W2 [h2][padRowOdd(h1)] (BF16).
 __host__ __device__ constexpr size_t fusedSmemF(int in, int h1, int h2, int batch) {
-    return sizeof(float) * ((size_t)batch * in + (size_t)batch * h1) +
-           sizeof(__nv_bfloat16) * ((size_t)h1 * in + (size_t)h2 * h1);
+    return sizeof(float) * ((size_t)batch * padRow(in) + (size_t)batch * padRowOdd(h1)) +
+           sizeof(__nv_bfloat16) * ((size_t)h1 * padRow(in) + (size_t)h2 * padRowOdd(h1));
 }
-// Shared memory of kernel A: a2, the dY slice, the W3 slice (BF16).
+// Shared memory of kernel A: a2 [B][padRowOdd(h2)], dY [B][32] (floats), W3 slice [32][padRowOdd(h2)] (BF16).
 __host__ __device__ constexpr size_t fusedSmemA(int h2, int batch) {
-    return sizeof(float) * ((size_t)batch * h2 + (size_t)batch * kFusedOutSlice) +
-           sizeof(__nv_bfloat16) * ((size_t)kFusedOutSlice * h2);
+    return sizeof(float) * ((size_t)batch * padRowOdd(h2) + (size_t)batch * kFusedOutSlice) +
+           sizeof(__nv_bfloat16) * ((size_t)kFusedOutSlice * padRowOdd(h2));
 }
 static_assert(fusedSmemF(kFusedMaxIn, kFusedMaxHidden, kFusedMaxHidden, kFusedMaxBatch) <= 227 * 1024,
               "kernel F's shared memory must fit one CTA");
 static_assert(fusedSmemA(kFusedMaxHidden, kFusedMaxBatch) <= 48 * 1024, "kernel A needs no shared-memory opt-in");
 
-// Hidden layers of the batch, once; products accumulated in increasing k.
+// Eight BF16 values (16 bytes) as floats.
+__device__ __forceinline__ void bf16x8(const __nv_bfloat16* p, float* f) {
+    const uint4 v = *reinterpret_cast<const uint4*>(p);
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        f[2 * i] = __uint_as_float(w[i] << 16);
+        f[2 * i + 1] = __uint_as_float(w[i] & 0xFFFF0000u);
+    }
+}
+
+// Dot product of a BF16 weight row and a float row of n elements (both padded
+// with zeros to a multiple of 8, 16-byte aligned), accumulated in increasing k.
+__device__ __forceinline__ float dotRow(const __nv_bfloat16* w, const float* x, int n) {
+    float s = 0.0f;
+    for (int k = 0; k < n; k += 8) {
+        float wf[8];
+        bf16x8(w + k, wf);
+        const float4 x0 = *reinterpret_cast<const float4*>(x + k);
+        const float4 x1 = *reinterpret_cast<const float4*>(x + k + 4);
+        s = fmaf(wf[0], x0.x, s);
+        s = fmaf(wf[1], x0.y, s);
+        s = fmaf(wf[2], x0.z, s);
+        s = fmaf(wf[3], x0.w, s);
+        s = fmaf(wf[4], x1.x, s);
+        s = fmaf(wf[5], x1.y, s);
+        s = fmaf(wf[6], x1.z, s);
+        s = fmaf(wf[7], x1.w, s);
+    }
+    return s;
+}
+
+// Hidden layers of the batch, once. Thread t computes unit j = t % 64 of the
+// batch rows t / 64, t / 64 + 16, ...; zero padding adds nothing to the sums.
 __global__ void __launch_bounds__(1024) trainForwardKernel(FusedNet n) {
     extern __shared__ __align__(16) unsigned char smemRaw[];
     const int B = n.batch, IN = n.in, H1 = n.h1, H2 = n.h2;
+    const int INP = padRow(IN), H1P = padRowOdd(H1);
     float* xs = reinterpret_cast<float*>(smemRaw);
-    float* a1 = xs + (size_t)B * IN;
-    __nv_bfloat16* w1 = reinterpret_cast<__nv_bfloat16*>(a1 + (size_t)B * H1);
-    __nv_bfloat16* w2 = w1 + (size_t)H1 * IN;
+    float* a1 = xs + (size_t)B * INP;
+    __nv_bfloat16* w1 = reinterpret_cast<__nv_bfloat16*>(a1 + (size_t)B * H1P);
+    __nv_bfloat16* w2 = w1 + (size_t)H1 * INP;
     pdlWait();
     pdlTrigger();
     const int t = threadIdx.x, nt = blockDim.x;
-    for (int i = t; i < B * IN; i += nt) {
-        const int b = i / IN, k = i - b * IN;
+    for (int b = 0; b < B; b++) {
         const long long r = n.rows ? n.rows[b] : b;
-        if ((r < 0 || r >= n.poolRows) && k == 0) atomicOr(n.badRows, 1);
-        const float v = n.xPool[poolRow(n, b) * IN + k];
-        xs[i] = v;
-        n.x[i] = v;
+        if (t == 0 && (r < 0 || r >= n.poolRows)) atomicOr(n.badRows, 1);
+        const float* src = n.xPool + poolRow(n, b) * IN;
+        for (int k = t; k < INP; k += nt) {
+            const float v = k < IN ? src[k] : 0.0f;
+            xs[(size_t)b * INP + k] = v;
+            if (k < IN) n.x[(size_t)b * IN + k] = v;
+        }
     }
-    for (int i = t; i < H1 * IN; i += nt) w1[i] = n.w16[n.oW1 + i];
-    for (int i = t; i < H2 * H1; i += nt) w2[i] = n.w16[n.oW2 + i];
+    for (int j = 0; j < H1; j++)
+        for (int k = t; k < INP; k += nt)
+            w1[(size_t)j * INP + k] = k < IN ? n.w16[n.oW1 + (long long)j * IN + k] : __float2bfloat16_rn(0.0f);
+    for (int i = t; i < H2 * H1P; i += nt) {
+        const int j = i / H1P, k = i - j * H1P;
+        w2[i] = k < H1 ? n.w16[n.oW2 + (long long)j * H1 + k] : __float2bfloat16_rn(0.0f);
+    }
+    for (int i = t; i < B * H1P; i += nt) a1[i] = 0.0f;
     __syncthreads();
-    for (int i = t; i < B * H1; i += nt) {
-        const int b = i / H1, j = i - b * H1;
-        const float* xr = xs + (size_t)b * IN;
-        const __nv_bfloat16* wr = w1 + (size_t)j * IN;
-        float s = 0.0f;
-        for (int k = 0; k < IN; k++) s = fmaf(__bfloat162float(wr[k]), xr[k], s);
-        const float z = s + __bfloat162float(n.w16[n.ob1 + j]);
-        const float a = gelu(z);
-        a1[i] = a;
-        n.z1[i] = z;
-        n.a1[i] = a;
+    const int j = t & 63;
+    for (int b = t >> 6; b < B; b += nt >> 6) {
+        if (j < H1) {
+            const float z = dotRow(w1 + (size_t)j * INP, xs + (size_t)b * INP, INP) + __bfloat162float(n.w16[n.ob1 + j]);
+            const float a = gelu(z);
+            a1[(size_t)b * H1P + j] = a;
+            n.z1[b * H1 + j] = z;
+            n.a1[b * H1 + j] = a;
+        }
     }
     __syncthreads();
-    for (int i = t; i < B * H2; i += nt) {
-        const int b = i / H2, j = i - b * H2;
-        const float* ar = a1 + (size_t)b * H1;
-        const __nv_bfloat16* wr = w2 + (size_t)j * H1;
-        float s = 0.0f;
-        for (int k = 0; k < H1; k++) s = fmaf(__bfloat162float(wr[k]), ar[k], s);
-        const float z = s + __bfloat162float(n.w16[n.ob2 + j]);
-        n.z2[i] = z;
-        n.a2[i] = gelu(z);
+    for (int b = t >> 6; b < B; b += nt >> 6) {
+        if (j < H2) {
+            const float z = dotRow(w2 + (size_t)j * H1P, a1 + (size_t)b * H1P, H1P) +
+                            __bfloat162float(n.w16[n.ob2 + j]);
+            n.z2[b * H2 + j] = z;
+            n.a2[b * H2 + j] = gelu(z);
+        }
     }
 }
 
+// One CTA (8 warps) per 32 outputs: lane q owns output o0 + q.
 __global__ void __launch_bounds__(kFusedThreads) trainOutputKernel(FusedNet n) {
     extern __shared__ __align__(16) unsigned char smemRaw[];
     __shared__ float red[kFusedThreads / 32];
-    const int B = n.batch, H2 = n.h2;
-    float* a2 = reinterpret_cast<float*>(smemRaw);
-    float* dy = a2 + (size_t)B * H2;                                                          // [B][slice]
-    __nv_bfloat16* w3 = reinterpret_cast<__nv_bfloat16*>(dy + (size_t)B * kFusedOutSlice);   // [slice][H2]
+    const int B = n.batch, H2 = n.h2, H2P = padRowOdd(H2);
+    float* a2 = reinterpret_cast<float*>(smemRaw);                                            // [B][H2P]
+    float* dy = a2 + (size_t)B * H2P;                                                         // [B][32]
+    __nv_bfloat16* w3 = reinterpret_cast<__nv_bfloat16*>(dy + (size_t)B * kFusedOutSlice);   // [32][H2P]
     pdlWait();
     pdlTrigger();
-    const int t = threadIdx.x, nt = blockDim.x;
+    const int t = threadIdx.x, nt = blockDim.x, lane = t & 31, warp = t >> 5, nw = nt >> 5;
     const int o0 = blockIdx.x * kFusedOutSlice;
     const int no = min(kFusedOutSlice, n.out - o0);
-    for (int i = t; i < B * H2; i += nt) a2[i] = n.a2[i];
-    for (int i = t; i < no * H2; i += nt) w3[i] = n.w16[n.oW3 + (long long)o0 * H2 + i];
+    for (int i = t; i < B * H2P; i += nt) {
+        const int b = i / H2P, k = i - b * H2P;
+        a2[i] = k < H2 ? n.a2[b * H2 + k] : 0.0f;
+    }
+    for (int i = t; i < kFusedOutSlice * H2P; i += nt) {
+        const int q = i / H2P, k = i - q * H2P;
+        w3[i] = (q < no && k < H2) ? n.w16[n.oW3 + (long long)(o0 + q) * H2 + k] : __float2bfloat16_rn(0.0f);
+    }
     __syncthreads();
-    // Output slice: y, the weighted error and dY = 2 w (y - t) * lossScale.
+    // y, the weighted error and dY = 2 w (y - t) * lossScale for (batch row b, output lane).
     float l = 0.0f;
-    for (int i = t; i < B * kFusedOutSlice; i += nt) {
-        const int b = i / kFusedOutSlice, q = i - b * kFusedOutSlice;
+    const int q = lane;
+    const float wo = (q < no && n.outWeights) ? n.outWeights[o0 + q] : 1.0f;
+    const float bias = q < no ? __bfloat162float(n.w16[n.ob3 + o0 + q]) : 0.0f;
+    for (int b = warp; b < B; b += nw) {
         float d = 0.0f;
         if (q < no) {
-            const int o = o0 + q;
-            const float* ar = a2 + (size_t)b * H2;
-            const __nv_bfloat16* wr = w3 + (size_t)q * H2;
-            float s = 0.0f;
-            for (int k = 0; k < H2; k++) s = fmaf(__bfloat162float(wr[k]), ar[k], s);
-            const float y = s + __bfloat162float(n.w16[n.ob3 + o]);
-            const float e = y - n.tPool[poolRow(n, b) * n.out + o];
-            const float wo = n.outWeights ? n.outWeights[o] : 1.0f;
+            const float y = dotRow(w3 + (size_t)q * H2P, a2 + (size_t)b * H2P, H2P) + bias;
+            const float e = y - n.tPool[poolRow(n, b) * n.out + o0 + q];
             d = 2.0f * wo * e * n.lossScale;
             l = fmaf(wo * e, e, l);
         }
-        dy[i] = d;
+        dy[b * kFusedOutSlice + q] = d;
     }
     // The slice's loss, summed in a fixed order.
     for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xFFFFFFFFu, l, o);
-    if ((t & 31) == 0) red[t >> 5] = l;
+    if (lane == 0) red[warp] = l;
     __syncthreads();
     if (t == 0) {
         float sum = 0.0f;
-        for (int w = 0; w < nt / 32; w++) sum += red[w];
+        for (int w = 0; w < nw; w++) sum += red[w];
         n.lossPart[blockIdx.x] = sum;
     }
     // dL/da2 over this slice's rows: part[b][j] = sum_q dY[b][q] W3[q][j].
-    for (int i = t; i < B * H2; i += nt) {
-        const int b = i / H2, j = i - b * H2;
-        float sum = 0.0f;
-        for (int q = 0; q < no; q++)
-            sum = fmaf(dy[b * kFusedOutSlice + q], __bfloat162float(w3[(size_t)q * H2 + j]), sum);
-        n.da2Part[(size_t)blockIdx.x * B * H2 + i] = sum;
-    }
+    for (int b = warp; b < B; b += nw)
+        for (int jj = lane; jj < H2; jj += 32) {
+            float sum = 0.0f;
+            for (int qq = 0; qq < no; qq++)
+                sum = fmaf(dy[b * kFusedOutSlice + qq], __bfloat162float(w3[(size_t)qq * H2P + jj]), sum);
+            n.da2Part[((size_t)blockIdx.x * B + b) * H2 + jj] = sum;
+        }
     // Gradients of the slice's rows of W3 and b3 (batch order), then Adam.
-    for (int i = t; i < no * (H2 + 1); i += nt) {
-        const int q = i / (H2 + 1), j = i - q * (H2 + 1);
-        float g = 0.0f;
-        if (j < H2) {
-            for (int b = 0; b < B; b++) g = fmaf(dy[b * kFusedOutSlice + q], a2[(size_t)b * H2 + j], g);
-            adamUpdate(n, n.oW3 + (long long)(o0 + q) * H2 + j, g);
-        } else {
-            for (int b = 0; b < B; b++) g += dy[b * kFusedOutSlice + q];
-            adamUpdate(n, n.ob3 + o0 + q, g);
+    for (int qq = warp; qq < no; qq += nw) {
+        for (int jj = lane; jj < H2; jj += 32) {
+            float g = 0.0f;
+            for (int b = 0; b < B; b++) g = fmaf(dy[b * kFusedOutSlice + qq], a2[(size_t)b * H2P + jj], g);
+            adamUpdate(n, n.oW3 + (long long)(o0 + qq) * H2 + jj, g);
+        }
+        if (lane == 0) {
+            float g = 0.0f;
+            for (int b = 0; b < B; b++) g += dy[b * kFusedOutSlice + qq];
+            adamUpdate(n, n.ob3 + o0 + qq, g);
         }
     }
 }
 
+// Backward through the hidden layers (one CTA): dz2 = (sum over slices of
+// dL/da2) * GELU'(z2), dz1 = (dz2 . W2) * GELU'(z1), and the loss.
 __global__ void __launch_bounds__(1024) trainHiddenKernel(FusedNet n, int slices) {
     __shared__ float dz2s[kFusedMaxBatch * kFusedMaxHidden];
+    __shared__ __align__(16) __nv_bfloat16 w2s[kFusedMaxHidden * kFusedMaxHidden];   // [j][k]
     pdlWait();
     pdlTrigger();
     const int B = n.batch, H1 = n.h1, H2 = n.h2;
     const int t = threadIdx.x, nt = blockDim.x;
+    for (int i = t; i < H2 * H1; i += nt) w2s[i] = n.w16[n.oW2 + i];
     for (int i = t; i < B * H2; i += nt) {
         float sum = 0.0f;
         for (int g = 0; g < slices; g++) sum += n.da2Part[(size_t)g * B * H2 + i];
@@ -387,12 +439,12 @@ __global__ void __launch_bounds__(1024) trainHiddenKernel(FusedNet n, int slices
         n.dz2[i] = d;
     }
     __syncthreads();
-    for (int i = t; i < B * H1; i += nt) {
-        const int b = i / H1, k = i - b * H1;
+    const int k = t & 63;
+    for (int b = t >> 6; b < B; b += nt >> 6) {
+        if (k >= H1) continue;
         float sum = 0.0f;
-        for (int j = 0; j < H2; j++)
-            sum = fmaf(dz2s[b * H2 + j], __bfloat162float(n.w16[n.oW2 + (long long)j * H1 + k]), sum);
-        n.dz1[i] = sum * geluGrad(n.z1[i]);
+        for (int j = 0; j < H2; j++) sum = fmaf(dz2s[b * H2 + j], __bfloat162float(w2s[j * H1 + k]), sum);
+        n.dz1[b * H1 + k] = sum * geluGrad(n.z1[b * H1 + k]);
     }
     if (t == 0) {
         float sum = 0.0f;
