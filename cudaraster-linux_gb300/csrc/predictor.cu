@@ -309,22 +309,27 @@ __global__ void __launch_bounds__(1024) trainForwardKernel(FusedNet n) {
     float* a1 = xs + (size_t)B * INP;
     __nv_bfloat16* w1 = reinterpret_cast<__nv_bfloat16*>(a1 + (size_t)B * H1P);
     __nv_bfloat16* w2 = w1 + (size_t)H1 * INP;
+    __shared__ long long rowOf[kFusedMaxBatch];
     pdlWait();
     pdlTrigger();
     const int t = threadIdx.x, nt = blockDim.x;
-    for (int b = 0; b < B; b++) {
-        const long long r = n.rows ? n.rows[b] : b;
-        if (t == 0 && (r < 0 || r >= n.poolRows)) atomicOr(n.badRows, 1);
-        const float* src = n.xPool + poolRow(n, b) * IN;
-        for (int k = t; k < INP; k += nt) {
-            const float v = k < IN ? src[k] : 0.0f;
-            xs[(size_t)b * INP + k] = v;
-            if (k < IN) n.x[(size_t)b * IN + k] = v;
-        }
+    if (t < B) {
+        const long long r = n.rows ? n.rows[t] : t;
+        if (r < 0 || r >= n.poolRows) atomicOr(n.badRows, 1);
+        rowOf[t] = poolRow(n, t);
     }
-    for (int j = 0; j < H1; j++)
-        for (int k = t; k < INP; k += nt)
-            w1[(size_t)j * INP + k] = k < IN ? n.w16[n.oW1 + (long long)j * IN + k] : __float2bfloat16_rn(0.0f);
+    __syncthreads();
+    // Every element loaded independently of the others (flat loops).
+    for (int i = t; i < B * INP; i += nt) {
+        const int b = i / INP, k = i - b * INP;
+        const float v = k < IN ? n.xPool[rowOf[b] * IN + k] : 0.0f;
+        xs[i] = v;
+        if (k < IN) n.x[(size_t)b * IN + k] = v;
+    }
+    for (int i = t; i < H1 * INP; i += nt) {
+        const int j = i / INP, k = i - j * INP;
+        w1[i] = k < IN ? n.w16[n.oW1 + (long long)j * IN + k] : __float2bfloat16_rn(0.0f);
+    }
     for (int i = t; i < H2 * H1P; i += nt) {
         const int j = i / H1P, k = i - j * H1P;
         w2[i] = k < H1 ? n.w16[n.oW2 + (long long)j * H1 + k] : __float2bfloat16_rn(0.0f);
