@@ -197,7 +197,7 @@ constexpr int kFusedMaxIn = 320;
 constexpr int kFusedMaxHidden = 64;
 constexpr int kFusedMaxBatch = 64;
 constexpr int kFusedOutSlice = 32;
-constexpr int kFusedThreads = 256;
+constexpr int kFusedThreads = 1024;
 
 struct FusedNet {
     int in, h1, h2, out, batch;
@@ -361,6 +361,7 @@ __global__ void __launch_bounds__(1024) trainForwardKernel(FusedNet n) {
 __global__ void __launch_bounds__(kFusedThreads) trainOutputKernel(FusedNet n) {
     extern __shared__ __align__(16) unsigned char smemRaw[];
     __shared__ float red[kFusedThreads / 32];
+    __shared__ long long rowOf[kFusedMaxBatch];
     const int B = n.batch, H2 = n.h2, H2P = padRowOdd(H2);
     float* a2 = reinterpret_cast<float*>(smemRaw);                                            // [B][H2P]
     float* dy = a2 + (size_t)B * H2P;                                                         // [B][32]
@@ -370,6 +371,7 @@ __global__ void __launch_bounds__(kFusedThreads) trainOutputKernel(FusedNet n) {
     const int t = threadIdx.x, nt = blockDim.x, lane = t & 31, warp = t >> 5, nw = nt >> 5;
     const int o0 = blockIdx.x * kFusedOutSlice;
     const int no = min(kFusedOutSlice, n.out - o0);
+    if (t < B) rowOf[t] = poolRow(n, t);
     for (int i = t; i < B * H2P; i += nt) {
         const int b = i / H2P, k = i - b * H2P;
         a2[i] = k < H2 ? n.a2[b * H2 + k] : 0.0f;
@@ -388,7 +390,7 @@ __global__ void __launch_bounds__(kFusedThreads) trainOutputKernel(FusedNet n) {
         float d = 0.0f;
         if (q < no) {
             const float y = dotRow(w3 + (size_t)q * H2P, a2 + (size_t)b * H2P, H2P) + bias;
-            const float e = y - n.tPool[poolRow(n, b) * n.out + o0 + q];
+            const float e = y - n.tPool[rowOf[b] * n.out + o0 + q];
             d = 2.0f * wo * e * n.lossScale;
             l = fmaf(wo * e, e, l);
         }
@@ -411,17 +413,18 @@ __global__ void __launch_bounds__(kFusedThreads) trainOutputKernel(FusedNet n) {
                 sum = fmaf(dy[b * kFusedOutSlice + qq], __bfloat162float(w3[(size_t)qq * H2P + jj]), sum);
             n.da2Part[((size_t)blockIdx.x * B + b) * H2 + jj] = sum;
         }
-    // Gradients of the slice's rows of W3 and b3 (batch order), then Adam.
+    // Gradients of the slice's rows of W3 and b3 (batch order), then Adam:
+    // warp w takes row q = w (and its bias), its lanes the row's columns.
     for (int qq = warp; qq < no; qq += nw) {
-        for (int jj = lane; jj < H2; jj += 32) {
+        for (int jj = lane; jj <= H2; jj += 32) {
             float g = 0.0f;
-            for (int b = 0; b < B; b++) g = fmaf(dy[b * kFusedOutSlice + qq], a2[(size_t)b * H2P + jj], g);
-            adamUpdate(n, n.oW3 + (long long)(o0 + qq) * H2 + jj, g);
-        }
-        if (lane == 0) {
-            float g = 0.0f;
-            for (int b = 0; b < B; b++) g += dy[b * kFusedOutSlice + qq];
-            adamUpdate(n, n.ob3 + o0 + qq, g);
+            if (jj < H2) {
+                for (int b = 0; b < B; b++) g = fmaf(dy[b * kFusedOutSlice + qq], a2[(size_t)b * H2P + jj], g);
+                adamUpdate(n, n.oW3 + (long long)(o0 + qq) * H2 + jj, g);
+            } else {
+                for (int b = 0; b < B; b++) g += dy[b * kFusedOutSlice + qq];
+                adamUpdate(n, n.ob3 + o0 + qq, g);
+            }
         }
     }
 }
