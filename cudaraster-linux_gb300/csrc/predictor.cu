@@ -179,18 +179,19 @@ __global__ void roundBf16Kernel(const float* __restrict__ w, __nv_bfloat16* __re
 // ------------------------------------------------------ fused training step
 // One training step (or one gradient evaluation) in four launches instead of
 // a gather, six GEMMs, three bias reductions, the loss and Adam:
-//   F  (one CTA): gathers the batch and runs both hidden layers (z1, a1, z2,
-//      a2 into global memory);
-//   A  (one CTA per 32 outputs): its slice of the output layer, the weighted
+//   F  (one CTA per 8 units of hidden layer 1): gathers the batch and runs
+//      hidden layer 1 (z1, a1 into global memory);
+//   A  (one CTA per 32 outputs): hidden layer 2 (small, so every CTA runs
+//      it), its slice of the output layer, the weighted
 //      squared error and dY, the gradient of its rows of W3 / b3 (and their
 //      Adam update), and its part of dL/da2 = dY . W3 over its rows;
-//   B  (one CTA): dL/da2 summed over the A CTAs in CTA order, dz2,
+//   B  (one CTA per batch row): dL/da2 summed over the A CTAs in CTA order, dz2,
 //      da1 = dz2 . W2, dz1, and the loss;
 //   C  (one thread per parameter of the hidden layers): the gradients of W1,
 //      b1, W2, b2 (and their Adam update).
 // No launch reads a parameter that another CTA of the same launch updates:
-// W3 rows are read only by the CTA that owns them, W2 is read by B and
-// updated by C, W1 and the hidden biases are read by F only. Every sum runs
+// W3 rows are read only by the CTA that owns them, W2 and b2 are read by A
+// and B and updated by C, W1 and b1 are read by F only. Every sum runs
 // in a fixed order, so results do not depend on timing. Sizes: inputs <=
 // kFusedMaxIn, hidden layers <= kFusedMaxHidden, batch <= kFusedMaxBatch.
 constexpr int kFusedMaxIn = 320;
@@ -252,20 +253,21 @@ __device__ __forceinline__ long long poolRow(const FusedNet& n, int b) {
 __host__ __device__ constexpr int padRow(int n) { return (n + 7) & ~7; }
 __host__ __device__ constexpr int padRowOdd(int n) { return padRow(n) + 8; }   // 16 bytes more: 4 banks apart
 
-// Shared memory of kernel F: inputs [B][padRow(in)], a1 [B][padRowOdd(h1)] (floats),
-// W1 [h1][padRow(in)] and W2 [h2][padRowOdd(h1)] (BF16).
-__host__ __device__ constexpr size_t fusedSmemF(int in, int h1, int h2, int batch) {
-    return sizeof(float) * ((size_t)batch * padRow(in) + (size_t)batch * padRowOdd(h1)) +
-           sizeof(__nv_bfloat16) * ((size_t)h1 * padRow(in) + (size_t)h2 * padRowOdd(h1));
+// Shared memory of kernel F: inputs [B][padRow(in)] (floats), its W1 rows [kFusedUnits][padRow(in)] (BF16).
+constexpr int kFusedUnits = 8;   // hidden-layer-1 units per kernel F CTA
+__host__ __device__ constexpr size_t fusedSmemF(int in, int batch) {
+    return sizeof(float) * (size_t)batch * padRow(in) + sizeof(__nv_bfloat16) * (size_t)kFusedUnits * padRow(in);
 }
-// Shared memory of kernel A: a2 [B][padRowOdd(h2)], dY [B][32] (floats), W3 slice [32][padRowOdd(h2)] (BF16).
-__host__ __device__ constexpr size_t fusedSmemA(int h2, int batch) {
-    return sizeof(float) * ((size_t)batch * padRowOdd(h2) + (size_t)batch * kFusedOutSlice) +
-           sizeof(__nv_bfloat16) * ((size_t)kFusedOutSlice * padRowOdd(h2));
+// Shared memory of kernel A: a1 [B][padRowOdd(h1)], a2 [B][padRowOdd(h2)], dY [B][32] (floats),
+// W2 [h2][padRowOdd(h1)] and the W3 slice [32][padRowOdd(h2)] (BF16).
+__host__ __device__ constexpr size_t fusedSmemA(int h1, int h2, int batch) {
+    return sizeof(float) * ((size_t)batch * padRowOdd(h1) + (size_t)batch * padRowOdd(h2) +
+                            (size_t)batch * kFusedOutSlice) +
+           sizeof(__nv_bfloat16) * ((size_t)h2 * padRowOdd(h1) + (size_t)kFusedOutSlice * padRowOdd(h2));
 }
-static_assert(fusedSmemF(kFusedMaxIn, kFusedMaxHidden, kFusedMaxHidden, kFusedMaxBatch) <= 227 * 1024,
-              "kernel F's shared memory must fit one CTA");
-static_assert(fusedSmemA(kFusedMaxHidden, kFusedMaxBatch) <= 48 * 1024, "kernel A needs no shared-memory opt-in");
+static_assert(fusedSmemF(kFusedMaxIn, kFusedMaxBatch) <= 227 * 1024, "kernel F's shared memory must fit one CTA");
+static_assert(fusedSmemA(kFusedMaxHidden, kFusedMaxHidden, kFusedMaxBatch) <= 227 * 1024,
+              "kernel A's shared memory must fit one CTA");
 
 // Eight BF16 values (16 bytes) as floats.
 __device__ __forceinline__ void bf16x8(const __nv_bfloat16* p, float* f) {
@@ -299,86 +301,88 @@ __device__ __forceinline__ float dotRow(const __nv_bfloat16* w, const float* x, 
     return s;
 }
 
-// Hidden layers of the batch, once. Thread t computes unit j = t % 64 of the
-// batch rows t / 64, t / 64 + 16, ...; zero padding adds nothing to the sums.
-__global__ void __launch_bounds__(1024) trainForwardKernel(FusedNet n) {
+// Hidden layer 1: CTA c computes units kFusedUnits * c ... + kFusedUnits - 1
+// for every batch row (thread t: unit t % kFusedUnits, rows t / kFusedUnits,
+// + blockDim / kFusedUnits, ...); zero padding adds nothing to the sums. CTA 0
+// also keeps the gathered inputs for the weight gradients.
+__global__ void __launch_bounds__(256) trainForwardKernel(FusedNet n) {
     extern __shared__ __align__(16) unsigned char smemRaw[];
-    const int B = n.batch, IN = n.in, H1 = n.h1, H2 = n.h2;
-    const int INP = padRow(IN), H1P = padRowOdd(H1);
-    float* xs = reinterpret_cast<float*>(smemRaw);
-    float* a1 = xs + (size_t)B * INP;
-    __nv_bfloat16* w1 = reinterpret_cast<__nv_bfloat16*>(a1 + (size_t)B * H1P);
-    __nv_bfloat16* w2 = w1 + (size_t)H1 * INP;
     __shared__ long long rowOf[kFusedMaxBatch];
+    const int B = n.batch, IN = n.in, H1 = n.h1;
+    const int INP = padRow(IN);
+    float* xs = reinterpret_cast<float*>(smemRaw);
+    __nv_bfloat16* w1 = reinterpret_cast<__nv_bfloat16*>(xs + (size_t)B * INP);
     pdlWait();
     pdlTrigger();
     const int t = threadIdx.x, nt = blockDim.x;
+    const int j0 = blockIdx.x * kFusedUnits;
     if (t < B) {
         const long long r = n.rows ? n.rows[t] : t;
-        if (r < 0 || r >= n.poolRows) atomicOr(n.badRows, 1);
+        if (blockIdx.x == 0 && (r < 0 || r >= n.poolRows)) atomicOr(n.badRows, 1);
         rowOf[t] = poolRow(n, t);
     }
     __syncthreads();
-    // Every element loaded independently of the others (flat loops).
     for (int i = t; i < B * INP; i += nt) {
         const int b = i / INP, k = i - b * INP;
         const float v = k < IN ? n.xPool[rowOf[b] * IN + k] : 0.0f;
         xs[i] = v;
-        if (k < IN) n.x[(size_t)b * IN + k] = v;
+        if (blockIdx.x == 0 && k < IN) n.x[(size_t)b * IN + k] = v;
     }
-    for (int i = t; i < H1 * INP; i += nt) {
-        const int j = i / INP, k = i - j * INP;
-        w1[i] = k < IN ? n.w16[n.oW1 + (long long)j * IN + k] : __float2bfloat16_rn(0.0f);
-    }
-    for (int i = t; i < H2 * H1P; i += nt) {
-        const int j = i / H1P, k = i - j * H1P;
-        w2[i] = k < H1 ? n.w16[n.oW2 + (long long)j * H1 + k] : __float2bfloat16_rn(0.0f);
-    }
-    for (int i = t; i < B * H1P; i += nt) a1[i] = 0.0f;
-    __syncthreads();
-    const int j = t & 63;
-    for (int b = t >> 6; b < B; b += nt >> 6) {
-        if (j < H1) {
-            const float z = dotRow(w1 + (size_t)j * INP, xs + (size_t)b * INP, INP) + __bfloat162float(n.w16[n.ob1 + j]);
-            const float a = gelu(z);
-            a1[(size_t)b * H1P + j] = a;
-            n.z1[b * H1 + j] = z;
-            n.a1[b * H1 + j] = a;
-        }
+    for (int i = t; i < kFusedUnits * INP; i += nt) {
+        const int u = i / INP, k = i - u * INP;
+        w1[i] = (k < IN && j0 + u < H1) ? n.w16[n.oW1 + (long long)(j0 + u) * IN + k] : __float2bfloat16_rn(0.0f);
     }
     __syncthreads();
-    for (int b = t >> 6; b < B; b += nt >> 6) {
-        if (j < H2) {
-            const float z = dotRow(w2 + (size_t)j * H1P, a1 + (size_t)b * H1P, H1P) +
-                            __bfloat162float(n.w16[n.ob2 + j]);
-            n.z2[b * H2 + j] = z;
-            n.a2[b * H2 + j] = gelu(z);
-        }
+    const int u = t % kFusedUnits, j = j0 + u;
+    if (j >= H1) return;
+    const float bias = __bfloat162float(n.w16[n.ob1 + j]);
+    for (int b = t / kFusedUnits; b < B; b += nt / kFusedUnits) {
+        const float z = dotRow(w1 + (size_t)u * INP, xs + (size_t)b * INP, INP) + bias;
+        n.z1[b * H1 + j] = z;
+        n.a1[b * H1 + j] = gelu(z);
     }
 }
 
-// One CTA (8 warps) per 32 outputs: lane q owns output o0 + q.
+// One CTA per 32 outputs: lane q owns output o0 + q.
 __global__ void __launch_bounds__(kFusedThreads) trainOutputKernel(FusedNet n) {
     extern __shared__ __align__(16) unsigned char smemRaw[];
     __shared__ float red[kFusedThreads / 32];
     __shared__ long long rowOf[kFusedMaxBatch];
-    const int B = n.batch, H2 = n.h2, H2P = padRowOdd(H2);
-    float* a2 = reinterpret_cast<float*>(smemRaw);                                            // [B][H2P]
+    const int B = n.batch, H1 = n.h1, H2 = n.h2, H1P = padRowOdd(H1), H2P = padRowOdd(H2);
+    float* a1 = reinterpret_cast<float*>(smemRaw);                                            // [B][H1P]
+    float* a2 = a1 + (size_t)B * H1P;                                                         // [B][H2P]
     float* dy = a2 + (size_t)B * H2P;                                                         // [B][32]
-    __nv_bfloat16* w3 = reinterpret_cast<__nv_bfloat16*>(dy + (size_t)B * kFusedOutSlice);   // [32][H2P]
+    __nv_bfloat16* w2 = reinterpret_cast<__nv_bfloat16*>(dy + (size_t)B * kFusedOutSlice);   // [H2][H1P]
+    __nv_bfloat16* w3 = w2 + (size_t)H2 * H1P;                                                // [32][H2P]
     pdlWait();
     pdlTrigger();
     const int t = threadIdx.x, nt = blockDim.x, lane = t & 31, warp = t >> 5, nw = nt >> 5;
     const int o0 = blockIdx.x * kFusedOutSlice;
     const int no = min(kFusedOutSlice, n.out - o0);
     if (t < B) rowOf[t] = poolRow(n, t);
-    for (int i = t; i < B * H2P; i += nt) {
-        const int b = i / H2P, k = i - b * H2P;
-        a2[i] = k < H2 ? n.a2[b * H2 + k] : 0.0f;
+    for (int i = t; i < B * H1P; i += nt) {
+        const int b = i / H1P, k = i - b * H1P;
+        a1[i] = k < H1 ? n.a1[b * H1 + k] : 0.0f;
+    }
+    for (int i = t; i < H2 * H1P; i += nt) {
+        const int j = i / H1P, k = i - j * H1P;
+        w2[i] = k < H1 ? n.w16[n.oW2 + (long long)j * H1 + k] : __float2bfloat16_rn(0.0f);
     }
     for (int i = t; i < kFusedOutSlice * H2P; i += nt) {
         const int q = i / H2P, k = i - q * H2P;
         w3[i] = (q < no && k < H2) ? n.w16[n.oW3 + (long long)(o0 + q) * H2 + k] : __float2bfloat16_rn(0.0f);
+    }
+    __syncthreads();
+    // Hidden layer 2 (every CTA; CTA 0 keeps z2 for the backward pass).
+    for (int i = t; i < B * H2P; i += nt) {
+        const int b = i / H2P, j = i - b * H2P;
+        float a = 0.0f;
+        if (j < H2) {
+            const float z = dotRow(w2 + (size_t)j * H1P, a1 + (size_t)b * H1P, H1P) + __bfloat162float(n.w16[n.ob2 + j]);
+            a = gelu(z);
+            if (blockIdx.x == 0) n.z2[b * H2 + j] = z;
+        }
+        a2[i] = a;
     }
     __syncthreads();
     // y, the weighted error and dY = 2 w (y - t) * lossScale for (batch row b, output lane).
@@ -429,32 +433,30 @@ __global__ void __launch_bounds__(kFusedThreads) trainOutputKernel(FusedNet n) {
     }
 }
 
-// Backward through the hidden layers (one CTA): dz2 = (sum over slices of
-// dL/da2) * GELU'(z2), dz1 = (dz2 . W2) * GELU'(z1), and the loss.
-__global__ void __launch_bounds__(1024) trainHiddenKernel(FusedNet n, int slices) {
-    __shared__ float dz2s[kFusedMaxBatch * kFusedMaxHidden];
-    __shared__ __align__(16) __nv_bfloat16 w2s[kFusedMaxHidden * kFusedMaxHidden];   // [j][k]
+// Backward through the hidden layers, one CTA per batch row b (thread = unit):
+// dz2 = (sum over slices, in slice order, of dL/da2) * GELU'(z2),
+// dz1 = (dz2 . W2) * GELU'(z1); CTA 0 also sums the loss.
+__global__ void __launch_bounds__(kFusedMaxHidden) trainHiddenKernel(FusedNet n, int slices) {
+    __shared__ float dz2s[kFusedMaxHidden];
     pdlWait();
     pdlTrigger();
     const int B = n.batch, H1 = n.h1, H2 = n.h2;
-    const int t = threadIdx.x, nt = blockDim.x;
-    for (int i = t; i < H2 * H1; i += nt) w2s[i] = n.w16[n.oW2 + i];
-    for (int i = t; i < B * H2; i += nt) {
+    const int t = threadIdx.x, b = blockIdx.x;
+    if (t < H2) {
+        const int i = b * H2 + t;
         float sum = 0.0f;
         for (int g = 0; g < slices; g++) sum += n.da2Part[(size_t)g * B * H2 + i];
         const float d = sum * geluGrad(n.z2[i]);
-        dz2s[i] = d;
+        dz2s[t] = d;
         n.dz2[i] = d;
     }
     __syncthreads();
-    const int k = t & 63;
-    for (int b = t >> 6; b < B; b += nt >> 6) {
-        if (k >= H1) continue;
+    if (t < H1) {
         float sum = 0.0f;
-        for (int j = 0; j < H2; j++) sum = fmaf(dz2s[b * H2 + j], __bfloat162float(w2s[j * H1 + k]), sum);
-        n.dz1[b * H1 + k] = sum * geluGrad(n.z1[b * H1 + k]);
+        for (int j = 0; j < H2; j++) sum = fmaf(dz2s[j], __bfloat162float(n.w16[n.oW2 + j * H1 + t]), sum);
+        n.dz1[b * H1 + t] = sum * geluGrad(n.z1[b * H1 + t]);
     }
-    if (t == 0) {
+    if (b == 0 && t == 0) {
         float sum = 0.0f;
         for (int g = 0; g < slices; g++) sum += n.lossPart[g];
         *n.loss = sum * n.lossScale;
@@ -853,12 +855,15 @@ cr_status trainFused(cr_predictor* p, const float* xPool, const float* tPool, in
     static cr::OncePerDevice attribute;
     attribute.run([] {
         cudaFuncSetAttribute(trainForwardKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)fusedSmemF(kFusedMaxIn, kFusedMaxHidden, kFusedMaxHidden, kFusedMaxBatch));
+                             (int)fusedSmemF(kFusedMaxIn, kFusedMaxBatch));
+        cudaFuncSetAttribute(trainOutputKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)fusedSmemA(kFusedMaxHidden, kFusedMaxHidden, kFusedMaxBatch));
     });
-    cudaError_t e = cr::launchKernel(trainForwardKernel, 1, 1024, fusedSmemF(n.in, n.h1, n.h2, batch), s, false, n);
+    cudaError_t e = cr::launchKernel(trainForwardKernel, (n.h1 + kFusedUnits - 1) / kFusedUnits, 256,
+                                     fusedSmemF(n.in, batch), s, false, n);
     if (e == cudaSuccess)
-        e = cr::launchKernel(trainOutputKernel, p->slices, kFusedThreads, fusedSmemA(n.h2, batch), s, true, n);
-    if (e == cudaSuccess) e = cr::launchKernel(trainHiddenKernel, 1, 1024, 0, s, true, n, p->slices);
+        e = cr::launchKernel(trainOutputKernel, p->slices, kFusedThreads, fusedSmemA(n.h1, n.h2, batch), s, true, n);
+    if (e == cudaSuccess) e = cr::launchKernel(trainHiddenKernel, batch, kFusedMaxHidden, 0, s, true, n, p->slices);
     if (e == cudaSuccess)
         e = cr::launchKernel(trainWeightsKernel, (unsigned)((p->oW3 + 255) / 256), 256, 0, s, true, n);
     return e == cudaSuccess ? CR_OK : CR_ERR_CUDA;
