@@ -70,6 +70,16 @@ struct FineWarpSmem {
     F32 shared[32];
 };
 
+// A triangle of the visibility path's batch in 12 words: edge functions
+// E0-2, A0-2, B0-2 (see TileEdges) and depth plane zx, zy, zb. Lanes read a
+// record with three 128-bit loads: all lanes the same one (a broadcast) on
+// the large-triangle path; on the pair path lanes of a quarter warp read
+// consecutive records, whose 48-byte stride puts any eight of them on
+// distinct banks.
+struct TriRec {
+    uint4 q[3];   // E0 E1 E2 A0 | A1 A2 B0 B1 | B2 zx zy zb
+};
+
 // The visibility path's per-warp state: no separate depth array (a key's high
 // word is its sample's depth) and only the triangle words it reads.
 template <int S>
@@ -77,10 +87,7 @@ struct FineVisSmem {
     static constexpr int kTileWords = 64 << S;
     U32 color[kTileWords];
     U64 key[kTileWords];        // depth << 32 | order (order << 8 | coverage mask with MSAA)
-    S32 E[3][32];
-    S32 A[3][32];
-    S32 B[3][32];
-    U32 z[3][32];               // depth plane (zx, zy, zb) of the batch's triangles
+    TriRec rec[32];             // the batch's triangles
     U32 box[32];                // bx0 | by0 << 4 | w << 8 of each small triangle's pixel box
     U32 mul[32];                // ceil(2^16 / w)
     S32 pairEnd[32];            // inclusive prefix of the pair counts
@@ -364,15 +371,9 @@ __device__ __forceinline__ void fineTiles(const DrawDev& d, int group, S32 tileB
                             const S32 w = bx1 - bx0 + 1;
                             const S32 cnt = w * (by1 - by0 + 1);
                             big = cnt > selfPixels;
-#pragma unroll
-                            for (int k = 0; k < 3; k++) {
-                                sm.E[k][lane] = te.E[k];
-                                sm.A[k][lane] = te.A[k];
-                                sm.B[k][lane] = te.B[k];
-                            }
-                            sm.z[0][lane] = q0.x;
-                            sm.z[1][lane] = q0.y;
-                            sm.z[2][lane] = q0.z;
+                            sm.rec[lane].q[0] = make_uint4((U32)te.E[0], (U32)te.E[1], (U32)te.E[2], (U32)te.A[0]);
+                            sm.rec[lane].q[1] = make_uint4((U32)te.A[1], (U32)te.A[2], (U32)te.B[0], (U32)te.B[1]);
+                            sm.rec[lane].q[2] = make_uint4((U32)te.B[2], q0.x, q0.y, q0.z);
                             if (!big) {
                                 n = cnt;
                                 sm.box[lane] = (U32)bx0 | (U32)by0 << 4 | (U32)w << 8;
@@ -406,15 +407,16 @@ __device__ __forceinline__ void fineTiles(const DrawDev& d, int group, S32 tileB
                     const S32 w = (S32)(bw >> 8);
                     const S32 q = (S32)(((U32)k * sm.mul[j]) >> 16);
                     const S32 px = (S32)(bw & 0xFu) + k - q * w, py = (S32)((bw >> 4) & 0xFu) + q;
-                    const S32 E[3] = {sm.E[0][j], sm.E[1][j], sm.E[2][j]};
-                    const S32 A[3] = {sm.A[0][j], sm.A[1][j], sm.A[2][j]};
-                    const S32 B[3] = {sm.B[0][j], sm.B[1][j], sm.B[2][j]};
+                    const uint4 r0 = sm.rec[j].q[0], r1 = sm.rec[j].q[1], r2 = sm.rec[j].q[2];
+                    const S32 E[3] = {(S32)r0.x, (S32)r0.y, (S32)r0.z};
+                    const S32 A[3] = {(S32)r0.w, (S32)r1.x, (S32)r1.y};
+                    const S32 B[3] = {(S32)r1.z, (S32)r1.w, (S32)r2.x};
                     const U32 smask = sampleMaskOf<S>(E, A, B, px, py);
                     if (!smask) continue;
                     const U32 order = (U32)(batch + j + 1);
                     const U64 low = packed ? (order << 8 | smask) : order;
                     const U32 X = (U32)(tx * 8 + px), Y = (U32)(ty * 8 + py);
-                    const U32 zx = sm.z[0][j], zy = sm.z[1][j], zb = sm.z[2][j];
+                    const U32 zx = r2.y, zy = r2.z, zb = r2.w;
 #pragma unroll
                     for (int i = 0; i < NS; i++) {
                         if (!(smask >> i & 1)) continue;
@@ -424,16 +426,46 @@ __device__ __forceinline__ void fineTiles(const DrawDev& d, int group, S32 tileB
                     }
                 }
                 __syncwarp();
-                // Larger triangles: the whole warp, one at a time (each lane
-                // owns its two pixels, so plain stores suffice).
+                // Larger triangles: the whole warp, one at a time, in batch
+                // order (each lane owns its two pixels, so plain stores
+                // suffice). At one sample a lane keeps its two keys in
+                // registers over all of them: the row below is 4 pixels
+                // (64 subpixels) down, so its edge values are the first
+                // row's plus 64 B and its depth the first's plus 4 zy; a
+                // sample is covered iff no edge value is negative, i.e. iff
+                // their OR is not.
                 const S32 px = lane & 7, py0 = lane >> 3, py1 = py0 + 4;
                 const U32 pX = (U32)(tx * 8 + px), pY0 = (U32)(ty * 8 + py0), pY1 = pY0 + 4;
-                for (U32 m = __ballot_sync(0xFFFFFFFFu, big); m; m &= m - 1) {
-                    const int j = __ffs(m) - 1;
-                    const S32 E[3] = {sm.E[0][j], sm.E[1][j], sm.E[2][j]};
-                    const S32 A[3] = {sm.A[0][j], sm.A[1][j], sm.A[2][j]};
-                    const S32 B[3] = {sm.B[0][j], sm.B[1][j], sm.B[2][j]};
-                    const U32 zx = sm.z[0][j], zy = sm.z[1][j], zb = sm.z[2][j];
+                U32 bigMask = __ballot_sync(0xFFFFFFFFu, big);
+                if (S == 0 && bigMask) {
+                    const int idx0 = py0 * 8 + px, idx1 = idx0 + 32;
+                    U64 k0 = sm.key[idx0], k1 = sm.key[idx1];
+                    const S32 qx = px << kSubpixelLog2, qy = py0 << kSubpixelLog2;
+                    for (; bigMask; bigMask &= bigMask - 1) {
+                        const int j = __ffs(bigMask) - 1;
+                        const uint4 r0 = sm.rec[j].q[0], r1 = sm.rec[j].q[1], r2 = sm.rec[j].q[2];
+                        const S32 e00 = (S32)r0.x + (S32)r0.w * qx + (S32)r1.z * qy;
+                        const S32 e01 = (S32)r0.y + (S32)r1.x * qx + (S32)r1.w * qy;
+                        const S32 e02 = (S32)r0.z + (S32)r1.y * qx + (S32)r2.x * qy;
+                        const S32 e10 = e00 + ((S32)r1.z << (kSubpixelLog2 + 2));
+                        const S32 e11 = e01 + ((S32)r1.w << (kSubpixelLog2 + 2));
+                        const S32 e12 = e02 + ((S32)r2.x << (kSubpixelLog2 + 2));
+                        const U32 z0 = r2.y * pX + r2.z * pY0 + r2.w, z1 = z0 + (r2.z << 2);
+                        const U32 order = (U32)(batch + j + 1);
+                        const U64 key0 = ((U64)z0 << 32) | order, key1 = ((U64)z1 << 32) | order;
+                        if ((e00 | e01 | e02) >= 0 && key0 < k0) k0 = key0;
+                        if ((e10 | e11 | e12) >= 0 && key1 < k1) k1 = key1;
+                    }
+                    sm.key[idx0] = k0;
+                    sm.key[idx1] = k1;
+                }
+                for (; bigMask; bigMask &= bigMask - 1) {
+                    const int j = __ffs(bigMask) - 1;
+                    const uint4 r0 = sm.rec[j].q[0], r1 = sm.rec[j].q[1], r2 = sm.rec[j].q[2];
+                    const S32 E[3] = {(S32)r0.x, (S32)r0.y, (S32)r0.z};
+                    const S32 A[3] = {(S32)r0.w, (S32)r1.x, (S32)r1.y};
+                    const S32 B[3] = {(S32)r1.z, (S32)r1.w, (S32)r2.x};
+                    const U32 zx = r2.y, zy = r2.z, zb = r2.w;
                     const U32 order = (U32)(batch + j + 1);
 #pragma unroll
                     for (int half = 0; half < 2; half++) {
