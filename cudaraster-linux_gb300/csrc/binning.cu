@@ -58,6 +58,7 @@ __device__ __forceinline__ S32 blockExclusiveScan(S32 v, S32* scratch, S32* tota
 // Geometry of a cell grid (bins of the viewport, or tiles inside one bin).
 struct Grid {
     S32 halfW, halfH, cellLog2;
+    bool centerOnly;          // one sample per pixel: boxes of pixel centres (cellBox)
     S32 cx0, cy0, cx1, cy1;   // clamp window (inclusive)
     S32 stride;               // cells per row of the local index space
 };
@@ -83,7 +84,7 @@ __device__ __forceinline__ S32 stageItems(const DrawDev& d, const Grid& gr, bool
     uint4 h = make_uint4(0u, 0u, 0u, 0u);
     if (valid) {
         h = __ldg(&d.triHeader[entrySlot(entry, d.triHeader)]);
-        b = cellBox(geomFromHeader(h), gr.halfW, gr.halfH, gr.cellLog2, gr.cx0, gr.cy0, gr.cx1, gr.cy1);
+        b = cellBox(geomFromHeader(h), gr.halfW, gr.halfH, gr.cellLog2, gr.cx0, gr.cy0, gr.cx1, gr.cy1, gr.centerOnly);
         n = b.count();
     }
     gs.entry[lane] = entry;
@@ -150,6 +151,7 @@ __device__ __forceinline__ Grid binGrid(const InstanceDev* in, int binLog2) {
     gr.halfW = __ldg(&in->width) << (kSubpixelLog2 - 1);
     gr.halfH = __ldg(&in->height) << (kSubpixelLog2 - 1);
     gr.cellLog2 = binLog2 + kTileLog2 + kSubpixelLog2;
+    gr.centerOnly = __ldg(&in->samplesLog2) == 0;
     gr.cx0 = 0;
     gr.cy0 = 0;
     gr.cx1 = __ldg(&in->widthBins) - 1;
@@ -450,6 +452,7 @@ __device__ __forceinline__ Grid tileGrid(const UnitInfo& ui, int binLog2) {
     gr.halfW = __ldg(&ui.in->width) << (kSubpixelLog2 - 1);
     gr.halfH = __ldg(&ui.in->height) << (kSubpixelLog2 - 1);
     gr.cellLog2 = kTileLog2 + kSubpixelLog2;
+    gr.centerOnly = __ldg(&ui.in->samplesLog2) == 0;
     gr.cx0 = ui.bx << binLog2;
     gr.cy0 = ui.by << binLog2;
     gr.cx1 = min(gr.cx0 + side - 1, __ldg(&ui.in->widthTiles) - 1);

@@ -1,6 +1,7 @@
 // binning.cuh -- conservative triangle-vs-rectangle tests shared by the bin
 // and coarse stages. A triangle is kept for a bin / tile unless its bounding
-// box misses it or one edge has the whole rectangle strictly outside; exact
+// box (at one sample per pixel: the box of the pixel centres inside it) misses
+// it or one edge has the whole rectangle strictly outside; exact
 // per-sample coverage is decided later by the fine stage, so a kept triangle
 // that covers no sample changes no output bit. The reference makes the same
 // conservative choice with its bbox fast paths and corner tests
@@ -46,13 +47,21 @@ struct CellBox {
     __device__ __forceinline__ bool small() const { return (hx - lx) <= 1 && (hy - ly) <= 1; }
 };
 
+// With one sample per pixel (centerOnly) the box is that of the pixel centres
+// inside the vertex box: pixel p's centre lies at 16 p + 8 subpixels from the
+// viewport's left edge, so the first centre at or right of x is pixel
+// (x + 7) >> 4 and the last at or left of x is (x - 8) >> 4 (x from that edge);
+// a cell whose pixel centres all miss the vertex box holds no sample the fine
+// stage could cover. With MSAA the samples spread over the pixel, and the box
+// is that of the vertices.
 __device__ __forceinline__ CellBox cellBox(const TriGeom& g, S32 halfW, S32 halfH, int cellLog2,
-                                           S32 cx0, S32 cy0, S32 cx1, S32 cy1) {
+                                           S32 cx0, S32 cy0, S32 cx1, S32 cy1, bool centerOnly) {
+    const S32 lo = centerOnly ? 7 : 0, hi = centerOnly ? 8 : 0;
     CellBox b;
-    b.lx = max((min3i(g.x0, g.x1, g.x2) + halfW) >> cellLog2, cx0);
-    b.hx = min((max3i(g.x0, g.x1, g.x2) + halfW) >> cellLog2, cx1);
-    b.ly = max((min3i(g.y0, g.y1, g.y2) + halfH) >> cellLog2, cy0);
-    b.hy = min((max3i(g.y0, g.y1, g.y2) + halfH) >> cellLog2, cy1);
+    b.lx = max((min3i(g.x0, g.x1, g.x2) + halfW + lo) >> cellLog2, cx0);
+    b.hx = min((max3i(g.x0, g.x1, g.x2) + halfW - hi) >> cellLog2, cx1);
+    b.ly = max((min3i(g.y0, g.y1, g.y2) + halfH + lo) >> cellLog2, cy0);
+    b.hy = min((max3i(g.y0, g.y1, g.y2) + halfH - hi) >> cellLog2, cy1);
     return b;
 }
 

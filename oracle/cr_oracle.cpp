@@ -760,12 +760,16 @@ bool tri_touches_rect(const TriGeom& g, S64 rx0, S64 ry0, S64 rx1, S64 ry1) {
 // Cells of the rule in the window [wx0, wx1] x [wy0, wy1] of a grid with cells
 // of 2^cellLog2 subpixels.
 template <class Fn>
-void rule_cells(const Viewport& vp, const TriGeom& g, int cellLog2, S32 wx0, S32 wy0, S32 wx1, S32 wy1, Fn fn) {
+void rule_cells(const Viewport& vp, int samplesLog2, const TriGeom& g, int cellLog2, S32 wx0, S32 wy0, S32 wx1,
+                S32 wy1, Fn fn) {
     const S32 hw = vp.width << (SUBPIXEL_LOG2 - 1), hh = vp.height << (SUBPIXEL_LOG2 - 1);
-    S32 lx = std::max((min3(g.v0x, g.v1x, g.v2x) + hw) >> cellLog2, wx0);
-    S32 hx = std::min((max3(g.v0x, g.v1x, g.v2x) + hw) >> cellLog2, wx1);
-    S32 ly = std::max((min3(g.v0y, g.v1y, g.v2y) + hh) >> cellLog2, wy0);
-    S32 hy = std::min((max3(g.v0y, g.v1y, g.v2y) + hh) >> cellLog2, wy1);
+    // One sample per pixel: the box of the pixel centres (16 p + 8 from the
+    // viewport's edge) inside the vertex box; with MSAA the vertex box.
+    const S32 lo = samplesLog2 == 0 ? 7 : 0, hi = samplesLog2 == 0 ? 8 : 0;
+    S32 lx = std::max((min3(g.v0x, g.v1x, g.v2x) + hw + lo) >> cellLog2, wx0);
+    S32 hx = std::min((max3(g.v0x, g.v1x, g.v2x) + hw - hi) >> cellLog2, wx1);
+    S32 ly = std::max((min3(g.v0y, g.v1y, g.v2y) + hh + lo) >> cellLog2, wy0);
+    S32 hy = std::min((max3(g.v0y, g.v1y, g.v2y) + hh - hi) >> cellLog2, wy1);
     if (lx > hx || ly > hy) return;
     const bool small = hx - lx <= 1 && hy - ly <= 1;
     const S64 side = (S64)1 << cellLog2;
@@ -987,7 +991,8 @@ int or_render(const or_pipe* p, const float* vertices, const int32_t* indices,
 //   kind 0 / 2: bins / tiles, exact -- entries covering at least one sample of
 //               the cell's pixels (the per-sample rule above);
 //   kind 1 / 3: bins / tiles, the binning rule of the GPU stages -- the
-//               entry's bounding box, in cells and clamped to the cell window
+//               entry's bounding box (at one sample per pixel the box of the
+//               pixel centres inside it), in cells and clamped to the cell window
 //               (the viewport's bins; for tiles the tiles of the bin), contains
 //               the cell, and either the clamped box spans at most 2x2 cells or
 //               no edge has the whole cell rectangle strictly outside; a tile
@@ -1040,13 +1045,13 @@ int64_t or_queue_lists(const or_pipe* p, const float* vertices, const int32_t* i
                     }
                 }
         } else {
-            rule_cells(vp, it.g, binCell, 0, 0, wb - 1, hb - 1, [&](S32 bx, S32 by) {
+            rule_cells(vp, s, it.g, binCell, 0, 0, wb - 1, hb - 1, [&](S32 bx, S32 by) {
                 if (bins) {
                     lists[(size_t)by * wb + bx].push_back(it.entry);
                     return;
                 }
                 const S32 x0 = bx << bin_log2, y0 = by << bin_log2;
-                rule_cells(vp, it.g, tileCell, x0, y0, std::min(x0 + side - 1, wt - 1), std::min(y0 + side - 1, ht - 1),
+                rule_cells(vp, s, it.g, tileCell, x0, y0, std::min(x0 + side - 1, wt - 1), std::min(y0 + side - 1, ht - 1),
                            [&](S32 tx, S32 ty) { lists[(size_t)ty * wt + tx].push_back(it.entry); });
             });
         }
