@@ -267,7 +267,8 @@ def run_flythrough_plain(ft: FlyThrough, frames: range, tuning: dict | None = No
 def run_flythrough_predicted(ft: FlyThrough, frames: int, train_frames: int = 50, tuning: dict | None = None,
                              checksums: bool = False, keep: tuple = (), train_steps: int = 4,
                              online_every: int = 4, seed: int = 0, lr: float = 3e-4, ahead: int = 2,
-                             min_margin: float = 0.02, margin_factor: float = 2.0, capacity_scale: float = 1.0):
+                             min_margin: float = 0.02, margin_factor: float = 2.0, capacity_scale: float = 1.0,
+                             layer_streams: bool = True):
     """The first `train_frames` frames are plain (synchronous draws) and train
     one predictor per layer on the counts they emit. Later frames are drawn
     asynchronously into queues sized from predictions made `ahead` (= 2)
@@ -278,8 +279,11 @@ def run_flythrough_predicted(ft: FlyThrough, frames: int, train_frames: int = 50
     overflowed is redrawn through the plain overflow-detect-and-rerun path (on
     separate contexts, so the queued frame's counts survive) before its
     surfaces are reused, and the predictor steps are redone. capacity_scale
-    (tests) scales the capacities given to the draws. Returns wall times,
-    misses and the per-frame record."""
+    (tests) scales the capacities given to the draws. With layer_streams each
+    layer draws on its own stream, after the layer below it in the same frame:
+    the layers have their own contexts and consecutive frames their own
+    surfaces, so frame f's water layer may run beside frame f + 1's terrain.
+    Returns wall times, misses and the per-frame record."""
     import time
     if ahead != 2:
         raise ValueError("the pipelined loop predicts two frames ahead")
@@ -287,6 +291,7 @@ def run_flythrough_predicted(ft: FlyThrough, frames: int, train_frames: int = 50
     S = torch.cuda.current_stream()
     L = len(ft.layers)
     Q = [torch.cuda.Stream() for _ in range(L)]
+    D = [S] + [torch.cuda.Stream() if layer_streams else S for _ in range(L - 1)]
     crs = ft.contexts(tuning)
     fallback = ft.contexts(tuning)
     preds = None
@@ -303,12 +308,15 @@ def run_flythrough_predicted(ft: FlyThrough, frames: int, train_frames: int = 50
         stream. prev: the frame whose step must finish before a layer's
         contexts are drawn again."""
         for k, cr in enumerate(cset):
+            st = D[k]
             if prev is not None:
-                S.wait_event(ev_pred[k][prev % R])
-            ft.draw_layer(cr, k, f, S, sync)
+                st.wait_event(ev_pred[k][prev % R])
+            if k > 0 and st is not D[k - 1]:
+                st.wait_event(ev_draw[k - 1][f % R])    # a layer draws over the one below it
+            ft.draw_layer(cr, k, f, st, sync)
+            ev_draw[k][f % R].record(st)
             if preds is None:
                 return
-            ev_draw[k][f % R].record(S)
             Q[k].wait_event(ev_draw[k][f % R])
             preds[k].step(cr, f, ft.camera_delta(f, f + ahead), Q[k])
             ev_pred[k][f % R].record(Q[k])
