@@ -49,7 +49,7 @@ typedef enum cr_status {
     CR_ERR_CUDA = 6,             /* a CUDA runtime call failed (see cr_last_error)       */
     CR_ERR_TIMEOUT = 7,          /* a device-side bounded wait gave up                   */
     CR_ERR_OUT_OF_MEMORY = 8,
-    CR_ERR_UNSUPPORTED = 9       /* feature not available in this build                  */
+    CR_ERR_UNSUPPORTED = 9       /* feature not supported by this library                 */
 } cr_status;
 
 /* Render mode flags, as RenderModeFlag_* in src/cudaraster/cuda/PixelPipe.hpp:30-35. */
