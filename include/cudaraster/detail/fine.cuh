@@ -88,9 +88,8 @@ struct FineVisSmem {
     U32 color[kTileWords];
     U64 key[kTileWords];        // depth << 32 | order (order << 8 | coverage mask with MSAA)
     TriRec rec[32];             // the batch's triangles
-    U32 box[32];                // bx0 | by0 << 4 | w << 8 of each small triangle's pixel box
-    U32 mul[32];                // ceil(2^16 / w)
-    S32 pairEnd[32];            // inclusive prefix of the pair counts
+    U32 box[32];                // bx0 | by0 << 4 | w << 8 | ceil(2^16 / w) << 12: a small triangle's pixel box
+    S32 head[32];               // batch triangle whose pairs start at position i of the current pass
     U32 winners[kTileWords];    // resolve: (pixel | first sample << 6 | samples won << 9)
     F32 shared[32];
 };
@@ -348,14 +347,16 @@ __device__ __forceinline__ void fineTiles(const DrawDev& d, int group, S32 tileB
             if constexpr (kVisibility) {
                 // ---- Visibility. Every (triangle, pixel) pair of the batch's
                 // triangles whose pixel box has at most selfPixels pixels is
-                // dealt to the lanes in turn (pair p of the batch: its
-                // triangle j by a search over the prefix of box sizes, its
-                // pixel by an exact multiply-shift division by the box width;
-                // a lane walking its own triangle's box measured slower, even
-                // for boxes of one or two pixels); larger triangles are
-                // rasterized by the whole warp, two pixels per lane. Keys
-                // resolve by atomic minimum, so the order pairs are taken in
-                // does not change a bit.
+                // dealt to the lanes in turn, 32 pairs a pass: pair p's
+                // triangle is the last one whose pairs start at or before p
+                // (one OR over the warp marks the pass's starts, the
+                // triangle of the previous pass's last pair carries over),
+                // its pixel follows by an exact multiply-shift division by
+                // the box width (a lane walking its own triangle's box
+                // measured slower, even for boxes of one or two pixels);
+                // larger triangles are rasterized by the whole warp, two
+                // pixels per lane. Keys resolve by atomic minimum, so the
+                // order pairs are taken in does not change a bit.
                 S32 n = 0;
                 bool big = false;
                 if (batch + lane < count) {
@@ -376,14 +377,14 @@ __device__ __forceinline__ void fineTiles(const DrawDev& d, int group, S32 tileB
                             sm.rec[lane].q[2] = make_uint4((U32)te.B[2], q0.x, q0.y, q0.z);
                             if (!big) {
                                 n = cnt;
-                                sm.box[lane] = (U32)bx0 | (U32)by0 << 4 | (U32)w << 8;
                                 // Row of box pixel k: (k * ceil(2^16 / w)) >> 16, exact for k < 64, w <= 8.
-                                sm.mul[lane] = (65536u + (U32)w - 1u) / (U32)w;
+                                sm.box[lane] = (U32)bx0 | (U32)by0 << 4 | (U32)w << 8 |
+                                               ((65536u + (U32)w - 1u) / (U32)w) << 12;
                             }
                         }
                     }
                 }
-                S32 P = 0;
+                S32 P = 0, myStart = 0;
                 if (__any_sync(0xFFFFFFFFu, n > 0)) {
                     S32 incl = n;
 #pragma unroll
@@ -391,21 +392,32 @@ __device__ __forceinline__ void fineTiles(const DrawDev& d, int group, S32 tileB
                         const S32 t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
                         if (lane >= o) incl += t;
                     }
-                    sm.pairEnd[lane] = incl;
+                    myStart = incl - n;
                     P = __shfl_sync(0xFFFFFFFFu, incl, 31);
                 }
                 __syncwarp();
+                S32 carryJ = 0, carryStart = 0;   // triangle (and its first pair) of the last pair so far
                 for (S32 base = 0; base < P; base += 32) {
+                    const bool starts = n > 0 && myStart >= base && myStart < base + 32;
+                    if (starts) sm.head[myStart - base] = lane;
+                    const U32 startMask = __reduce_or_sync(0xFFFFFFFFu, starts ? 1u << (myStart - base) : 0u);
+                    __syncwarp();
+                    const U32 upTo = startMask & (0xFFFFFFFFu >> (31 - lane));
+                    S32 j = carryJ, first = carryStart;
+                    if (upTo) {
+                        const int h = 31 - __clz(upTo);
+                        j = sm.head[h];
+                        first = base + h;
+                    }
+                    carryJ = __shfl_sync(0xFFFFFFFFu, j, 31);
+                    carryStart = __shfl_sync(0xFFFFFFFFu, first, 31);
+                    __syncwarp();   // every lane has read head before the next pass rewrites it
                     const S32 p = base + lane;
                     if (p >= P) continue;
-                    int j = 0;
-#pragma unroll
-                    for (int s2 = 16; s2 > 0; s2 >>= 1)
-                        if (sm.pairEnd[j + s2 - 1] <= p) j += s2;
-                    const S32 k = p - (j ? sm.pairEnd[j - 1] : 0);
+                    const S32 k = p - first;
                     const U32 bw = sm.box[j];
-                    const S32 w = (S32)(bw >> 8);
-                    const S32 q = (S32)(((U32)k * sm.mul[j]) >> 16);
+                    const S32 w = (S32)((bw >> 8) & 0xFu);
+                    const S32 q = (S32)(((U32)k * (bw >> 12)) >> 16);
                     const S32 px = (S32)(bw & 0xFu) + k - q * w, py = (S32)((bw >> 4) & 0xFu) + q;
                     const uint4 r0 = sm.rec[j].q[0], r1 = sm.rec[j].q[1], r2 = sm.rec[j].q[2];
                     const S32 E[3] = {(S32)r0.x, (S32)r0.y, (S32)r0.z};
