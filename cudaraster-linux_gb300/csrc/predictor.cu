@@ -221,7 +221,6 @@ struct FusedNet {
     float* z1;                      // [batch][h1]
     float* a1;
     float* z2;                      // [batch][h2]
-    float* a2;
     float* dz1;
     float* dz2;
     float* da2Part;                 // [numOutSlices][batch][h2]
@@ -845,7 +844,6 @@ cr_status trainFused(cr_predictor* p, const float* xPool, const float* tPool, in
     n.z1 = p->z1;
     n.a1 = p->a1;
     n.z2 = p->z2;
-    n.a2 = p->a2;
     n.dz1 = p->dz1;
     n.dz2 = p->dz2;
     n.da2Part = p->da2Part;
