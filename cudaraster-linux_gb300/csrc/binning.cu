@@ -262,7 +262,9 @@ __device__ __forceinline__ ChunkInfo chunkInfo(const DrawDev& d, int chunk) {
 }
 
 // Persistent warps over chunks: each chunk's entry count per bin, written to
-// the (bin, chunk) matrix where not zero (the matrix is zero between draws).
+// the (bin, chunk) matrix where not zero (the matrix is zero between draws),
+// and, when d.binStageCap > 0, its (bin, entry) pairs in list order for the
+// scatter pass (as many as fit; their total in binStageCount).
 __global__ void __launch_bounds__(kWalkThreads) binCountKernel(DrawDev d) {
     pdlWait();
     pdlTrigger();
@@ -271,7 +273,9 @@ __global__ void __launch_bounds__(kWalkThreads) binCountKernel(DrawDev d) {
     __shared__ GroupSmem s_group[kWalkWarps];
     if (__ldg(&d.counters->overflow) & kOverflowSubtris) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const U32 ltMask = (1u << lane) - 1u;
     S32* cnt = s_cells + warp * d.maxBins;
+    GroupSmem& gs = s_group[warp];
     for (;;) {
         const int chunk = warpNextUnit(&d.counters->binWork[0]);
         if (chunk >= d.totalChunks) break;
@@ -279,9 +283,18 @@ __global__ void __launch_bounds__(kWalkThreads) binCountKernel(DrawDev d) {
         const Grid gr = binGrid(c.in, d.binLog2);
         for (int b = lane; b < c.nb; b += 32) cnt[b] = 0;
         __syncwarp();
-        walkSlice(d, gr, c.t0, c.t1, s_ring[warp], s_group[warp], [&](bool hit, int cell, int, U32 peers) {
+        U64* stage = d.binStage + (S64)chunk * d.binStageCap;
+        S32 staged = 0;   // pairs of the chunk so far (uniform)
+        walkSlice(d, gr, c.t0, c.t1, s_ring[warp], gs, [&](bool hit, int cell, int j, U32 peers) {
             if (hit && (peers >> lane) == 1u) cnt[cell] += __popc(peers);
+            if (d.binStageCap > 0) {
+                const U32 hits = __ballot_sync(0xFFFFFFFFu, hit);
+                const S32 pos = staged + __popc(hits & ltMask);
+                if (hit && pos < d.binStageCap) stage[pos] = (U64)(U32)cell << 32 | gs.entry[j];
+                staged += __popc(hits);
+            }
         });
+        if (lane == 0 && d.binStageCap > 0) d.binStageCount[chunk] = staged;
         S32* out = d.chunkBinCount + __ldg(&c.in->chunkCountBase) + c.local;
         const S64 nc = __ldg(&c.in->numChunks);
         for (int b = lane; b < c.nb; b += 32) {
@@ -378,7 +391,10 @@ __global__ void __launch_bounds__(kBinThreads) binScanKernel(DrawDev d) {
 }
 
 // Persistent warps over chunks: writes each chunk's entries into the bin
-// lists, from the chunk's offset in every bin it touches.
+// lists, from the chunk's offset in every bin it touches: from the pairs the
+// count pass recorded, 32 at a time (a pair's rank in its bin is the bin's
+// running index plus the lower lanes of the batch on the same bin), or, for a
+// chunk whose pairs did not fit, by walking its triangles again.
 __global__ void __launch_bounds__(kWalkThreads) binScatterKernel(DrawDev d) {
     pdlWait();
     pdlTrigger();
@@ -400,6 +416,24 @@ __global__ void __launch_bounds__(kWalkThreads) binScatterKernel(DrawDev d) {
         const S32 binBase = __ldg(&c.in->binBase);
         for (int b = lane; b < c.nb; b += 32) run[b] = __ldg(&d.binStart[binBase + b]) + __ldg(&offs[b]);
         __syncwarp();
+        const S32 staged = d.binStageCap > 0 ? __ldcg(&d.binStageCount[chunk]) : -1;
+        if (staged >= 0 && staged <= d.binStageCap) {
+            const U64* stage = d.binStage + (S64)chunk * d.binStageCap;
+            for (S32 i0 = 0; i0 < staged; i0 += 32) {
+                const bool valid = i0 + lane < staged;
+                const U64 pr = valid ? __ldcg(&stage[i0 + lane]) : 0ull;
+                const int cell = (int)(pr >> 32);
+                const U32 peers = __match_any_sync(0xFFFFFFFFu, valid ? (U32)cell : 0x80000000u + (U32)lane);
+                if (valid) {
+                    const S64 idx = (S64)run[cell] + __popc(peers & ltMask);
+                    if (idx < d.maxBinEntries) d.binList[idx] = (U32)pr;
+                }
+                __syncwarp();
+                if (valid && (peers >> lane) == 1u) run[cell] += __popc(peers);
+                __syncwarp();
+            }
+            continue;
+        }
         walkSlice(d, gr, c.t0, c.t1, s_ring[warp], gs, [&](bool hit, int cell, int j, U32 peers) {
             if (hit) {
                 const S64 idx = (S64)run[cell] + __popc(peers & ltMask);
@@ -461,7 +495,10 @@ __device__ __forceinline__ Grid tileGrid(const UnitInfo& ui, int binLog2) {
     return gr;
 }
 
-// Persistent warps over coarse units (taken dynamically): per-unit tile counts.
+// Persistent warps over coarse units (taken dynamically): per-unit tile
+// counts, and, for units below d.tileStageUnits, their (tile, entry) pairs in
+// list order for the scatter pass (as many as fit; their total in
+// tileStageCount).
 __global__ void __launch_bounds__(kCoarseThreads) coarseCountKernel(DrawDev d) {
     pdlWait();
     pdlTrigger();
@@ -472,6 +509,7 @@ __global__ void __launch_bounds__(kCoarseThreads) coarseCountKernel(DrawDev d) {
     const int tpb = 1 << (2 * d.binLog2);
     S32* cnt = smem + warp * tpb;
     GroupSmem& gs = s_group[warp];
+    const U32 ltMask = (1u << lane) - 1u;
     const S32 numUnits = (S32)min((S64)__ldg(&d.counters->numUnits), d.maxUnits);
     const S32 unitEntries = __ldg(&d.counters->unitEntries);
     for (;;) {
@@ -482,18 +520,35 @@ __global__ void __launch_bounds__(kCoarseThreads) coarseCountKernel(DrawDev d) {
         const Grid gr = tileGrid(ui, d.binLog2);
         for (int t = lane; t < tpb; t += 32) cnt[t] = 0;
         __syncwarp();
+        const bool record = u < d.tileStageUnits;
+        U64* stage = d.tileStage + (S64)u * d.tileStageCap;
+        S32 staged = 0;   // pairs of the unit so far (uniform)
+        // Records the batch's hits in lane order, which is list order.
+        auto recordHits = [&](bool hit, int cell, U32 entry) {
+            const U32 hits = __ballot_sync(0xFFFFFFFFu, hit);
+            const S32 pos = staged + __popc(hits & ltMask);
+            if (hit && pos < d.tileStageCap) stage[pos] = (U64)(U32)cell << 32 | entry;
+            staged += __popc(hits);
+        };
         for (S32 e0 = ui.e0; e0 < ui.e1; e0 += 32) {
             S32 incl;
             int cell1;
             const bool valid = e0 + lane < ui.e1;
             const S32 P = stageItems(d, gr, valid, valid ? __ldg(&d.binList[e0 + lane]) : 0u, gs, incl, cell1);
-            if (P < 0 && cell1 >= 0) atomicAdd(&cnt[cell1], 1);
-            for (S32 p = lane; p < P; p += 32) {
-                int j, cell;
-                if (pairCell(gs, gr, p, j, cell)) atomicAdd(&cnt[cell], 1);
+            if (P < 0) {
+                if (cell1 >= 0) atomicAdd(&cnt[cell1], 1);
+                if (record) recordHits(cell1 >= 0, cell1, gs.entry[lane]);
+            }
+            for (S32 base = 0; base < P; base += 32) {
+                const S32 p = base + lane;
+                int j = 0, cell = 0;
+                const bool hit = p < P && pairCell(gs, gr, p, j, cell);
+                if (hit) atomicAdd(&cnt[cell], 1);
+                if (record) recordHits(hit, cell, gs.entry[j]);
             }
             __syncwarp();
         }
+        if (lane == 0 && record) d.tileStageCount[u] = staged;
         S32* out = d.unitTileCount + (S64)u * tpb;
         for (int t = lane; t < tpb; t += 32) out[t] = cnt[t];
         __syncwarp();
@@ -582,9 +637,11 @@ __global__ void __launch_bounds__(kBinThreads) coarseScanKernel(DrawDev d) {
 }
 
 // Persistent warps over coarse units (taken dynamically): writes tile list
-// entries. The group's pairs are taken 32 at a time in entry order; the rank
-// of a pair in its tile list is the tile's running index plus the number of
-// lower lanes of the batch on the same tile (a match on the tile index).
+// entries, from the pairs the count pass recorded or, for a unit whose pairs
+// were not recorded, by walking its entries again. Pairs are taken 32 at a
+// time in list order; the rank of a pair in its tile list is the tile's
+// running index plus the number of lower lanes of the batch on the same tile
+// (a match on the tile index).
 __global__ void __launch_bounds__(kCoarseThreads) coarseScatterKernel(DrawDev d) {
     pdlWait();
     pdlTrigger();
@@ -615,6 +672,24 @@ __global__ void __launch_bounds__(kCoarseThreads) coarseScatterKernel(DrawDev d)
             run[t] = v;
         }
         __syncwarp();
+        const S32 staged = u < d.tileStageUnits ? __ldcg(&d.tileStageCount[u]) : -1;
+        if (staged >= 0 && staged <= d.tileStageCap) {
+            const U64* stage = d.tileStage + (S64)u * d.tileStageCap;
+            for (S32 i0 = 0; i0 < staged; i0 += 32) {
+                const bool valid = i0 + lane < staged;
+                const U64 pr = valid ? __ldcg(&stage[i0 + lane]) : 0ull;
+                const int cell = (int)(pr >> 32);
+                const U32 peers = __match_any_sync(0xFFFFFFFFu, valid ? (U32)cell : 0x80000000u + (U32)lane);
+                if (valid) {
+                    const S64 idx = (S64)run[cell] + __popc(peers & ltMask);
+                    if (idx < d.maxTileEntries) d.tileList[idx] = (U32)pr;
+                }
+                __syncwarp();
+                if (valid && (peers >> lane) == 1u) run[cell] += __popc(peers);
+                __syncwarp();
+            }
+            continue;
+        }
         for (S32 e0 = ui.e0; e0 < ui.e1; e0 += 32) {
             S32 incl;
             int cell1;

@@ -123,6 +123,8 @@ struct cr_context {
     // Device memory.
     DevBuf triSubtris, triHeader, triData, chunkBinCount, chunkBinOffset, binCount, binStart, binUnitFirst, binList;
     DevBuf unitTileCount, tileCount, tileStart, tileList;
+    DevBuf binStage, binStageCount;     // bin pairs recorded by the count pass (DrawDev::binStage)
+    DevBuf tileStage, tileStageCount;   // tile pairs recorded by the coarse count pass (DrawDev::tileStage)
     // Per-draw block, written by one copy per draw: the zeroed Counters and one
     // fine-stage tile counter per pipe group, then the instance descriptors
     // and the prefix arrays.
@@ -265,7 +267,8 @@ cr_status cr_destroy(cr_context* ctx) {
     DevBuf* bufs[] = {&ctx->triSubtris, &ctx->triHeader, &ctx->triData, &ctx->chunkBinCount, &ctx->chunkBinOffset,
                       &ctx->binCount,
                       &ctx->binStart, &ctx->binUnitFirst, &ctx->binList, &ctx->unitTileCount,
-                      &ctx->tileCount, &ctx->tileStart, &ctx->tileList, &ctx->drawBlock};
+                      &ctx->tileCount, &ctx->tileStart, &ctx->tileList, &ctx->binStage, &ctx->binStageCount,
+                      &ctx->tileStage, &ctx->tileStageCount, &ctx->drawBlock};
     for (DevBuf* b : bufs) b->release();
     for (int i = 0; i < cr_context::kStageSlots; i++) {
         if (ctx->hostStage[i]) cudaFreeHost(ctx->hostStage[i]);
@@ -485,7 +488,7 @@ struct Plan {
     struct Group { const PipeDesc* pipe; int instBegin, instEnd; int64_t triBegin, triEnd; int32_t tileBegin, tileEnd; };
     std::vector<Group> groups;
     int64_t totalTris = 0, chunkCountEntries = 0;
-    int32_t totalBins = 0, totalTiles = 0, totalChunks = 0, maxBins = 0;
+    int32_t totalBins = 0, totalTiles = 0, totalChunks = 0, maxBins = 0, maxChunkTris = 0;
     int binLog2 = 4, unitEntries = 0;
     // Fused vertex transform (single draws only).
     const float* model = nullptr;
@@ -497,6 +500,20 @@ struct Plan {
 // the bin capacity; units sized on the device (unitEntries 0, at least 64
 // entries each) are also capped at 8M per-unit tile counters, and the device
 // grows the unit size until the draw's bin entries fit.
+// Bin pairs a chunk may record for the scatter pass: twice its triangles (a
+// chunk of small triangles makes about one bin entry per live triangle), at
+// most 1024; chunks with more are walked again by the scatter pass.
+int binStageCap(const Plan& plan) {
+    const int cap = std::min(2 * plan.maxChunkTris, 1024);
+    return (cap + 31) & ~31;
+}
+
+// Coarse units that record their tile pairs (units are sized on the device
+// to about two per resident coarse warp), and the pairs each may record;
+// later units and fuller ones are walked again by the coarse scatter pass.
+constexpr int kTileStageUnits = 16384;
+constexpr int kTileStageCap = 1024;
+
 int64_t unitCapacity(int64_t maxBinEntries, int unitEntries, int32_t totalBins, int tpb) {
     if (unitEntries > 0) return maxBinEntries / unitEntries + totalBins + 1;
     return std::min<int64_t>(maxBinEntries / 64, std::max<int64_t>(4096, (8 << 20) / tpb)) + totalBins + 1;
@@ -544,6 +561,7 @@ cr_status buildPlan(cr_context* ctx, const std::vector<HostInstance>& in, Plan& 
         if (chunkTris <= 0) chunkTris = autoChunk;
         d.chunkTris = chunkTris;
         d.numChunks = (d.numTris + chunkTris - 1) / chunkTris;
+        plan.maxChunkTris = std::max(plan.maxChunkTris, chunkTris);
         d.chunkBase = chunks;
         d.chunkCountBase = countBase;
         countBase += (int64_t)d.numChunks * nb;
@@ -626,6 +644,12 @@ cr_status ensureCapacity(cr_context* ctx, const Plan& plan) {
     CR_CUDA(ctx->tileCount.ensure((size_t)plan.totalTiles * 4), "cudaMalloc");
     CR_CUDA(ctx->tileStart.ensure((size_t)plan.totalTiles * 4), "cudaMalloc");
     CR_CUDA(ctx->tileList.ensure((size_t)ctx->maxTileEntries * 4), "cudaMalloc");
+    const int stageCap = binStageCap(plan);
+    CR_CUDA(ctx->binStage.ensure((size_t)std::max(plan.totalChunks, 1) * stageCap * 8), "cudaMalloc");
+    CR_CUDA(ctx->binStageCount.ensure((size_t)std::max(plan.totalChunks, 1) * 4), "cudaMalloc");
+    const int64_t stageUnits = std::min<int64_t>(maxUnits, kTileStageUnits);
+    CR_CUDA(ctx->tileStage.ensure((size_t)stageUnits * kTileStageCap * 8), "cudaMalloc");
+    CR_CUDA(ctx->tileStageCount.ensure((size_t)stageUnits * 4), "cudaMalloc");
     const size_t stage = drawBlockBytes(plan);
     CR_CUDA(ctx->drawBlock.ensure(stage), "cudaMalloc");
     if (stage > ctx->hostStageBytes) {
@@ -688,6 +712,13 @@ DrawDev makeDrawDev(cr_context* ctx, const Plan& plan) {
     d.tilePrefix = d.binPrefix + n1;
     d.counters = ctx->drawBlock.as<Counters>();
     d.fineTileCounter = (int32_t*)(ctx->drawBlock.as<char>() + sizeof(Counters));
+    d.binStage = ctx->binStage.as<U64>();
+    d.binStageCount = ctx->binStageCount.as<int32_t>();
+    d.binStageCap = binStageCap(plan);
+    d.tileStage = ctx->tileStage.as<U64>();
+    d.tileStageCount = ctx->tileStageCount.as<int32_t>();
+    d.tileStageCap = kTileStageCap;
+    d.tileStageUnits = (int32_t)std::min<int64_t>(d.maxUnits, kTileStageUnits);
     return d;
 }
 

@@ -137,6 +137,19 @@ struct DrawDev {
     const S64* triPrefix;     // triangles
     Counters* counters;
     S32* fineTileCounter;     // [pipe groups] fine-stage tile work counters
+    // Pairs recorded by the bin count pass for the bin scatter pass: chunk c's
+    // (bin << 32 | list entry) pairs in list order at binStage[c * binStageCap],
+    // their number in binStageCount[c]. A chunk with more pairs than
+    // binStageCap (or binStageCap 0) is walked again by the scatter pass.
+    U64* binStage;
+    S32* binStageCount;       // [totalChunks]
+    S32 binStageCap;
+    // Likewise for the coarse passes: unit u < tileStageUnits records its
+    // (tile of the bin << 32 | list entry) pairs at tileStage[u * tileStageCap].
+    U64* tileStage;
+    S32* tileStageCount;      // [tileStageUnits]
+    S32 tileStageCap;
+    S32 tileStageUnits;
 };
 
 // ------------------------------------------------------ instance lookup
