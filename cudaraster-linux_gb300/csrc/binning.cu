@@ -419,9 +419,11 @@ __global__ void __launch_bounds__(kWalkThreads) binScatterKernel(DrawDev d) {
         const S32 staged = d.binStageCap > 0 ? __ldcg(&d.binStageCount[chunk]) : -1;
         if (staged >= 0 && staged <= d.binStageCap) {
             const U64* stage = d.binStage + (S64)chunk * d.binStageCap;
+            U64 next = lane < staged ? __ldcg(&stage[lane]) : 0ull;   // the next batch loads during this one
             for (S32 i0 = 0; i0 < staged; i0 += 32) {
                 const bool valid = i0 + lane < staged;
-                const U64 pr = valid ? __ldcg(&stage[i0 + lane]) : 0ull;
+                const U64 pr = next;
+                if (i0 + 32 + lane < staged) next = __ldcg(&stage[i0 + 32 + lane]);
                 const int cell = (int)(pr >> 32);
                 const U32 peers = __match_any_sync(0xFFFFFFFFu, valid ? (U32)cell : 0x80000000u + (U32)lane);
                 if (valid) {
@@ -675,9 +677,11 @@ __global__ void __launch_bounds__(kCoarseThreads) coarseScatterKernel(DrawDev d)
         const S32 staged = u < d.tileStageUnits ? __ldcg(&d.tileStageCount[u]) : -1;
         if (staged >= 0 && staged <= d.tileStageCap) {
             const U64* stage = d.tileStage + (S64)u * d.tileStageCap;
+            U64 next = lane < staged ? __ldcg(&stage[lane]) : 0ull;   // the next batch loads during this one
             for (S32 i0 = 0; i0 < staged; i0 += 32) {
                 const bool valid = i0 + lane < staged;
-                const U64 pr = valid ? __ldcg(&stage[i0 + lane]) : 0ull;
+                const U64 pr = next;
+                if (i0 + 32 + lane < staged) next = __ldcg(&stage[i0 + 32 + lane]);
                 const int cell = (int)(pr >> 32);
                 const U32 peers = __match_any_sync(0xFFFFFFFFu, valid ? (U32)cell : 0x80000000u + (U32)lane);
                 if (valid) {
