@@ -66,7 +66,8 @@ struct FineWarpSmem {
     S32 tri[32];           // triangle index within the draw
     U32 covLo[32];
     U32 covHi[32];
-    S32 fragEnd[32];
+    S32 fragEnd[32];       // inclusive prefix of the small triangles' pair counts
+    S32 fragHead[32];      // batch triangle whose fragments start at position i of the current pass
     F32 shared[32];
 };
 
@@ -651,7 +652,8 @@ __device__ __forceinline__ void fineTiles(const DrawDev& d, int group, S32 tileB
                     S32 t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
                     if (lane >= o) inc += t;
                 }
-                sm.fragEnd[lane] = inc;
+                const S32 myFragStart = inc - pop;
+                S32 fragCarryJ = 0, fragCarryStart = 0;   // triangle (and its first fragment) of the last fragment so far
                 sm.covLo[lane] = myLo;
                 sm.covHi[lane] = myHi;
                 const S32 total = __shfl_sync(0xFFFFFFFFu, inc, 31);
@@ -664,16 +666,29 @@ __device__ __forceinline__ void fineTiles(const DrawDev& d, int group, S32 tileB
                     bool covered = false;
                     U32 sampleMask = 0;
                     U32 dz[NS];
+                    // Triangle of fragment f: the last one whose fragments start
+                    // at or before f (one OR over the warp marks the pass's
+                    // starts; the triangle of the previous pass's last fragment
+                    // carries over).
+                    const bool startsHere = pop > 0 && myFragStart >= pass && myFragStart < pass + 32;
+                    if (startsHere) sm.fragHead[myFragStart - pass] = lane;
+                    const U32 startMask = __reduce_or_sync(0xFFFFFFFFu, startsHere ? 1u << (myFragStart - pass) : 0u);
+                    __syncwarp();
+                    const U32 upTo = startMask & (0xFFFFFFFFu >> (31 - lane));
+                    int fragJ = fragCarryJ;
+                    S32 fragFirst = fragCarryStart;
+                    if (upTo) {
+                        const int h = 31 - __clz(upTo);
+                        fragJ = sm.fragHead[h];
+                        fragFirst = pass + h;
+                    }
+                    fragCarryJ = __shfl_sync(0xFFFFFFFFu, fragJ, 31);
+                    fragCarryStart = __shfl_sync(0xFFFFFFFFu, fragFirst, 31);
+                    __syncwarp();   // every lane has read fragHead before the next pass rewrites it
                     if (act) {
-                        // Triangle of fragment f: first j with fragEnd[j] > f.
-                        int lo = 0, hi = 31;
-                        while (lo < hi) {
-                            int mid = (lo + hi) >> 1;
-                            if (sm.fragEnd[mid] > f) hi = mid; else lo = mid + 1;
-                        }
-                        j = lo;
+                        j = fragJ;
                         const U32 cl = sm.covLo[j], ch = sm.covHi[j];
-                        const S32 k = f - (sm.fragEnd[j] - (S32)((__popc(cl) + __popc(ch)) * (kQuads ? 4 : 1)));
+                        const S32 k = f - fragFirst;
                         if (kQuads) {
                             int qbit = nthSetBit64(cl, ch, k >> 2);
                             pixel = qbit + (k & 1) + ((k & 2) << 2);  // findFragment, FineRaster.inl:417-427
