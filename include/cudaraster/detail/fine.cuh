@@ -20,6 +20,9 @@
 //   at a time in lane order, which is submission order. This replaces the
 //   reference's reliance on lock-step warps for same-address shared-memory
 //   races (FineRaster.inl:433-495, 758-851), undefined on sm_70 and later.
+//   With one sample, a depth test and a fragment shader that never discards,
+//   a fragment later in the batch than its pixel's minimum (depth, then
+//   position) is dropped before compaction: it would fail the LESS test.
 //
 // Visibility path (depth test on, blend shader that ignores the destination,
 //   fragment shader that never discards): the final colour and depth of a
@@ -66,6 +69,9 @@ struct FineWarpSmem {
     S32 tri[32];           // triangle index within the draw
     U32 covLo[32];
     U32 covHi[32];
+    // One sample, depth test on, no discard: each pixel's minimum of
+    // (depth << 32 | batch triangle) over the batch's covered fragments.
+    U64 batchMin[S == 0 ? 64 : 1];
     S32 fragEnd[32];       // inclusive prefix of the small triangles' pair counts
     S32 fragHead[32];      // batch triangle whose fragments start at position i of the current pass
     F32 shared[32];
@@ -514,6 +520,13 @@ __device__ __forceinline__ void fineTiles(const DrawDev& d, int group, S32 tileB
                 U32* pairMul = sm.pairMul;
                 sm.covLo[lane] = 0u;
                 sm.covHi[lane] = 0u;
+                // Batch filter (see step 2b): exact for single-sample depth-tested
+                // pipes whose fragment shader never discards.
+                constexpr bool kFilter = S == 0 && kDepth && !kQuads && !FW::FragmentShaderTraits<FS>::mayDiscard;
+                if constexpr (kFilter) {
+                    sm.batchMin[lane] = ~0ull;
+                    sm.batchMin[lane + 32] = ~0ull;
+                }
                 if (valid) {
                     U32 entry = __ldg(&d.tileList[start + batch + lane]);
                     U32 tri = entry >> 3, sub = entry & 7;
@@ -583,7 +596,10 @@ __device__ __forceinline__ void fineTiles(const DrawDev& d, int group, S32 tileB
                     }
                     if (kDepth && S == 0 && !kQuads && c) {
                         const U32 X = (U32)(tx * 8 + px), Y = (U32)(ty * 8 + py);
-                        c = (sm.td[0][j] * X + sm.td[1][j] * Y + sm.td[2][j]) < sm.depth[py * 8 + px];
+                        const U32 z = sm.td[0][j] * X + sm.td[1][j] * Y + sm.td[2][j];
+                        c = z < sm.depth[py * 8 + px];
+                        if constexpr (kFilter)
+                            if (c) atomicMin((unsigned long long*)&sm.batchMin[py * 8 + px], ((unsigned long long)z << 32) | (U32)j);
                     }
                     if (c) {
                         const int bit = py * 8 + px;
@@ -594,6 +610,11 @@ __device__ __forceinline__ void fineTiles(const DrawDev& d, int group, S32 tileB
                 if (self) {
                     myLo = sm.covLo[lane];
                     myHi = sm.covHi[lane];
+                }
+                U64 min0 = 0, min1 = 0;   // batch minima of this lane's pixels (lane, lane + 32)
+                if constexpr (kFilter) {
+                    min0 = sm.batchMin[lane];
+                    min1 = sm.batchMin[lane + 32];
                 }
                 __syncwarp();
                 const U32 coopMask = __ballot_sync(0xFFFFFFFFu, valid && !self);
@@ -624,9 +645,14 @@ __device__ __forceinline__ void fineTiles(const DrawDev& d, int group, S32 tileB
                         }
                         if (kDepth && S == 0 && !kQuads) {
                             const U32 zx = sm.td[0][j], zy = sm.td[1][j], zb = sm.td[2][j];
-                            const U32 z0 = zx * pX + zy * pY0 + zb;
+                            const U32 z0 = zx * pX + zy * pY0 + zb, z1 = z0 + zy * 4u;
                             c0 = c0 && (z0 < curZ0);
-                            c1 = c1 && (z0 + zy * 4u < curZ1);
+                            c1 = c1 && (z1 < curZ1);
+                            if constexpr (kFilter) {
+                                const U64 k0 = ((U64)z0 << 32) | (U32)j, k1 = ((U64)z1 << 32) | (U32)j;
+                                if (c0 && k0 < min0) min0 = k0;
+                                if (c1 && k1 < min1) min1 = k1;
+                            }
                         }
                         U32 lo = __ballot_sync(0xFFFFFFFFu, c0);
                         U32 hi = __ballot_sync(0xFFFFFFFFu, c1);
@@ -641,6 +667,29 @@ __device__ __forceinline__ void fineTiles(const DrawDev& d, int group, S32 tileB
                     c &= 0x0055005500550055ull;
                     myLo = (U32)c;
                     myHi = (U32)(c >> 32);
+                }
+                if constexpr (kFilter) {
+                    // ---- 2b. A fragment of pixel p later in the batch than p's
+                    // minimum (depth, then batch position) fails the in-order LESS
+                    // test: the minimum's own fragment passes (every earlier one is
+                    // deeper) and leaves the depth at or below the later one's, and
+                    // without discard nothing else changes it. Triangle j keeps
+                    // the pixels whose minimum is at j or later: a bit-sliced
+                    // comparison of the 5-bit positions (10 ballots) against j.
+                    const U32 w0 = min((U32)min0, 31u), w1 = min((U32)min1, 31u);
+                    U32 gtLo = 0u, eqLo = ~0u, gtHi = 0u, eqHi = ~0u;
+#pragma unroll
+                    for (int b = 4; b >= 0; b--) {
+                        const U32 pl = __ballot_sync(0xFFFFFFFFu, (w0 >> b) & 1u);
+                        const U32 ph = __ballot_sync(0xFFFFFFFFu, (w1 >> b) & 1u);
+                        const U32 jb = 0u - (((U32)lane >> b) & 1u);   // bit b of this lane's triangle j
+                        gtLo |= eqLo & pl & ~jb;
+                        eqLo &= ~(pl ^ jb);
+                        gtHi |= eqHi & ph & ~jb;
+                        eqHi &= ~(ph ^ jb);
+                    }
+                    myLo &= gtLo | eqLo;
+                    myHi &= gtHi | eqHi;
                 }
                 if (!valid) { myLo = 0; myHi = 0; }
 

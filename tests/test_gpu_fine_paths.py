@@ -8,7 +8,9 @@ match):
   are found through the carried start;
 * triangles of one constant depth, small and large mixed: every sample's
   winner is decided by list position alone, across batches and between the
-  pair loop and the large-triangle loop of one batch;
+  pair loop and the large-triangle loop of one batch (with src-over, only
+  each pixel's first fragment in list order passes the LESS test, the tie
+  the ordered path's batch filter must break by position);
 * slivers whose vertex boxes cross a tile or bin edge by less than half a
   pixel: at one sample per pixel those cells hold no pixel centre and are
   left out of the lists (the GPU lists must still equal the oracle's rule and
@@ -72,7 +74,8 @@ def _parity(pipe, sc, what):
     return cnt
 
 
-@pytest.mark.parametrize("pipe", ["PixelPipe_gouraud", "PixelPipe_gouraud_msaa4", "PixelPipe_gouraud_srcover"])
+@pytest.mark.parametrize("pipe", ["PixelPipe_gouraud", "PixelPipe_gouraud_msaa4", "PixelPipe_gouraud_srcover",
+                                  "PixelPipe_gouraud_additive"])
 def test_many_small_triangles_per_tile(cuda, pipe):
     rng = np.random.default_rng(71)
     W = H = 64
@@ -85,7 +88,7 @@ def test_many_small_triangles_per_tile(cuda, pipe):
     assert cnt["tile_entries"] > 60 * cnt["num_tiles"]
 
 
-@pytest.mark.parametrize("pipe", ["PixelPipe_gouraud", "PixelPipe_gouraud_msaa4"])
+@pytest.mark.parametrize("pipe", ["PixelPipe_gouraud", "PixelPipe_gouraud_msaa4", "PixelPipe_gouraud_srcover"])
 def test_constant_depth_mixed_sizes_keep_list_order(cuda, pipe):
     rng = np.random.default_rng(72)
     W = H = 96
