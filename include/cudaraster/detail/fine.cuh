@@ -276,13 +276,20 @@ __device__ __forceinline__ void fineTiles(const DrawDev& d, int group, S32 tileB
     if (__ldg(&d.counters->overflow)) return;
     const S32 selfPixels = d.fineSelfPixels > 0 ? d.fineSelfPixels : fineSelfPixelsDefault(S, kVisibility);
 
+    // A warp's tiles come from the counter in increasing order: its current
+    // instance stays valid until a tile reaches the next instance's first.
+    int ii = 0;
+    S32 instEnd = -1;
     for (;;) {
         S32 tile = 0;
         if (lane == 0) tile = atomicAdd(&d.fineTileCounter[group], 1);
         tile = __shfl_sync(0xFFFFFFFFu, tile, 0) + tileBegin;
         if (tile >= tileEnd) break;
 
-        const int ii = findInstance(d.tilePrefix, d.numInstances, tile);
+        if (tile >= instEnd) {
+            ii = findInstance(d.tilePrefix, d.numInstances, tile);
+            instEnd = __ldg(&d.tilePrefix[ii + 1]);   // the prefix has numInstances + 1 entries
+        }
         const InstanceDev* in = &d.inst[ii];
         const S32 wt = __ldg(&in->widthTiles);
         const S32 lt = tile - __ldg(&in->tileBase);
