@@ -728,7 +728,8 @@ static_assert(offsetof(Counters, coarseWork) == 6 * sizeof(int32_t) && sizeof(Co
 
 // Enqueues one draw of `plan` on `stream`. `stage` is pinned host memory for
 // the descriptors (the copy node reads it when a captured graph replays) and
-// `hostCounters` receives the device counters; with `events` false no stage
+// `hostCounters` (pinned) receives the device counters, written by the first
+// fine launch or copied after the draw; with `events` false no stage
 // events are recorded (graph capture).
 cr_status launchDrawWith(cr_context* ctx, const Plan& plan, cudaStream_t stream, void* stage, Counters* hostCounters,
                          bool events) {
@@ -756,16 +757,29 @@ cr_status launchDrawWith(cr_context* ctx, const Plan& plan, cudaStream_t stream,
     if (events) CR_CUDA(cudaEventRecord(ctx->ev[1], stream), "cudaEventRecord");
     CR_CUDA(launchBinning(d, plan.maxBins, ctx->numSMs, stream, events ? ctx->ev[2] : nullptr), "bin/coarse launch");
     if (events) CR_CUDA(cudaEventRecord(ctx->ev[3], stream), "cudaEventRecord");
+    // The first fine launch that has tiles writes the counters into the
+    // pinned host buffer (its device address); without one, a copy follows.
+    Counters* devHostCounters = nullptr;
+    if (cudaHostGetDevicePointer((void**)&devHostCounters, hostCounters, 0) != cudaSuccess) {
+        cudaGetLastError();
+        devHostCounters = nullptr;
+    }
     int warps = ctx->tuning.fine_warps > 0 ? ctx->tuning.fine_warps : 8;
     for (size_t gi = 0; gi < plan.groups.size(); gi++) {
         const Plan::Group& g = plan.groups[gi];
         int ctas = ctx->tuning.fine_ctas_per_sm > 0 ? ctx->tuning.fine_ctas_per_sm : g.pipe->fineOccupancy(warps);
-        CR_CUDA(g.pipe->launchFine(d, (int)gi, g.tileBegin, g.tileEnd, warps, ctas, ctx->numSMs, stream), "fine launch");
+        DrawDev dg = d;
+        if (devHostCounters && g.tileEnd > g.tileBegin) {
+            dg.hostCounters = devHostCounters;
+            devHostCounters = nullptr;
+        }
+        CR_CUDA(g.pipe->launchFine(dg, (int)gi, g.tileBegin, g.tileEnd, warps, ctas, ctx->numSMs, stream), "fine launch");
     }
     if (events) CR_CUDA(cudaEventRecord(ctx->ev[4], stream), "cudaEventRecord");
     ctx->eventsRecorded = events;
-    CR_CUDA(cudaMemcpyAsync(hostCounters, ctx->drawBlock.ptr, sizeof(Counters), cudaMemcpyDeviceToHost, stream),
-            "cudaMemcpyAsync");
+    if (devHostCounters)
+        CR_CUDA(cudaMemcpyAsync(hostCounters, ctx->drawBlock.ptr, sizeof(Counters), cudaMemcpyDeviceToHost, stream),
+                "cudaMemcpyAsync");
     return CR_OK;
 }
 
@@ -916,8 +930,8 @@ cr_status drawBatch(cr_context* ctx, const cr_instance* instances, int32_t count
 }  // namespace
 
 // A batched draw captured once into a CUDA graph and replayed per frame
-// (descriptor copies, counter resets, every kernel and the counter read-back
-// are graph nodes). Overflow cannot rerun inside a graph: the kernels skip the
+// (the descriptor copy with the counter resets and every kernel are graph
+// nodes; the first fine kernel writes the counters into pinned host memory). Overflow cannot rerun inside a graph: the kernels skip the
 // frame and raise a flag, and cr_batch_graph_counters reports it so the host
 // grows the queues and recaptures.
 struct cr_batch_graph {

@@ -150,6 +150,11 @@ struct DrawDev {
     S32* tileStageCount;      // [tileStageUnits]
     S32 tileStageCap;
     S32 tileStageUnits;
+    // Device address of the pinned host copy of the counters: the draw's first
+    // fine launch writes them there (every stage that changes them has
+    // finished by then), in place of a device-to-host copy after the draw.
+    // Null in every other launch.
+    Counters* hostCounters;
 };
 
 // ------------------------------------------------------ instance lookup

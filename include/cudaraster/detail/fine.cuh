@@ -273,6 +273,9 @@ __device__ __forceinline__ void fineTiles(const DrawDev& d, int group, S32 tileB
     const U32 ltMask = (1u << lane) - 1u;
     pdlWait();
     pdlTrigger();
+    if (d.hostCounters != nullptr && blockIdx.x == 0 && threadIdx.x < (int)(sizeof(Counters) / 4))
+        reinterpret_cast<volatile U32*>(d.hostCounters)[threadIdx.x] =
+            reinterpret_cast<const volatile U32*>(d.counters)[threadIdx.x];
     if (__ldg(&d.counters->overflow)) return;
     const S32 selfPixels = d.fineSelfPixels > 0 ? d.fineSelfPixels : fineSelfPixelsDefault(S, kVisibility);
 
