@@ -9,6 +9,7 @@
 // wrapper (CudaRaster.hpp) turns them into the reference's fail().
 #include "cudaraster.h"
 #include "cudaraster/detail/device.cuh"
+#include "cudaraster/detail/launch.h"
 #include "cudaraster/detail/pipe_registry.h"
 
 #include <algorithm>
@@ -726,6 +727,35 @@ static_assert(sizeof(InstanceDev) % 8 == 0, "the prefix arrays follow the descri
 static_assert(offsetof(Counters, coarseWork) == 6 * sizeof(int32_t) && sizeof(Counters) >= 8 * sizeof(int32_t),
               "cr_queue_counts exports the first 8 words of Counters");
 
+// A draw's block (zeroed counters, instance descriptors, prefix arrays) as a
+// kernel parameter: one CTA writes it to the device. Unlike a host-to-device
+// copy it lets the setup kernels, launched as programmatic dependents, be
+// scheduled behind it (they wait for it before their first access).
+template <int N>
+struct BlockWords {
+    uint32_t w[N];
+};
+template <int N>
+__global__ void __launch_bounds__(256) writeBlockKernel(const __grid_constant__ BlockWords<N> b, uint32_t* dst, int n) {
+    pdlTrigger();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = b.w[i];
+}
+template <int N>
+cudaError_t writeBlock(const void* src, void* dst, size_t bytes, cudaStream_t stream) {
+    BlockWords<N> b;
+    memcpy(b.w, src, bytes);
+    return launchKernel(writeBlockKernel<N>, 1, 256, 0, stream, false, b, (uint32_t*)dst, (int)(bytes / 4));
+}
+
+bool capturing(cudaStream_t s) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &st) != cudaSuccess) {
+        cudaGetLastError();
+        return true;
+    }
+    return st != cudaStreamCaptureStatusNone;
+}
+
 // Enqueues one draw of `plan` on `stream`. `stage` is pinned host memory for
 // the descriptors (the copy node reads it when a captured graph replays) and
 // `hostCounters` (pinned) receives the device counters, written by the first
@@ -734,8 +764,10 @@ static_assert(offsetof(Counters, coarseWork) == 6 * sizeof(int32_t) && sizeof(Co
 cr_status launchDrawWith(cr_context* ctx, const Plan& plan, cudaStream_t stream, void* stage, Counters* hostCounters,
                          bool events) {
     DrawDev d = makeDrawDev(ctx, plan);
-    // Stage the zeroed counters and the descriptors through pinned memory:
-    // one copy per draw.
+    // Stage the zeroed counters and the descriptors through pinned memory;
+    // a kernel parameter carries them to the device (a copy when the block is
+    // above 8 KB, and in a graph capture, whose copy node reads the stage at
+    // every replay).
     size_t n1 = plan.inst.size() + 1;
     size_t instBytes = sizeof(InstanceDev) * plan.inst.size();
     const size_t cb = counterBytes(plan);
@@ -747,9 +779,14 @@ cr_status launchDrawWith(cr_context* ctx, const Plan& plan, cudaStream_t stream,
     memcpy(hp + 8 * n1, plan.chunkPrefix.data(), 4 * n1);
     memcpy(hp + 12 * n1, plan.binPrefix.data(), 4 * n1);
     memcpy(hp + 16 * n1, plan.tilePrefix.data(), 4 * n1);
-    CR_CUDA(cudaMemcpyAsync(ctx->drawBlock.ptr, stage, cb + instBytes + kPrefixBytesPerInstance * n1,
-                            cudaMemcpyHostToDevice, stream),
-            "cudaMemcpyAsync");
+    const size_t blockBytes = cb + instBytes + kPrefixBytesPerInstance * n1;
+    if (blockBytes <= 1024 && !capturing(stream))
+        CR_CUDA(writeBlock<256>(stage, ctx->drawBlock.ptr, blockBytes, stream), "block write");
+    else if (blockBytes <= 8192 && !capturing(stream))
+        CR_CUDA(writeBlock<2048>(stage, ctx->drawBlock.ptr, blockBytes, stream), "block write");
+    else
+        CR_CUDA(cudaMemcpyAsync(ctx->drawBlock.ptr, stage, blockBytes, cudaMemcpyHostToDevice, stream),
+                "cudaMemcpyAsync");
 
     if (events) CR_CUDA(cudaEventRecord(ctx->ev[0], stream), "cudaEventRecord");
     for (const Plan::Group& g : plan.groups)
