@@ -730,7 +730,10 @@ static_assert(offsetof(Counters, coarseWork) == 6 * sizeof(int32_t) && sizeof(Co
 // A draw's block (zeroed counters, instance descriptors, prefix arrays) as a
 // kernel parameter: one CTA writes it to the device. Unlike a host-to-device
 // copy it lets the setup kernels, launched as programmatic dependents, be
-// scheduled behind it (they wait for it before their first access).
+// scheduled behind it (they wait for it before their first access). It needs
+// an SM slot, though: a queued draw whose stream runs beside another stream's
+// persistent fine kernel would wait for that kernel, where a copy would not,
+// so only blocking draws use it.
 template <int N>
 struct BlockWords {
     uint32_t w[N];
@@ -757,17 +760,18 @@ bool capturing(cudaStream_t s) {
 }
 
 // Enqueues one draw of `plan` on `stream`. `stage` is pinned host memory for
-// the descriptors (the copy node reads it when a captured graph replays) and
+// the descriptors (the copy node reads it when a captured graph replays;
+// with `writeKernel` a blocking draw's block goes as a kernel parameter) and
 // `hostCounters` (pinned) receives the device counters, written by the first
 // fine launch or copied after the draw; with `events` false no stage
 // events are recorded (graph capture).
 cr_status launchDrawWith(cr_context* ctx, const Plan& plan, cudaStream_t stream, void* stage, Counters* hostCounters,
-                         bool events) {
+                         bool events, bool writeKernel) {
     DrawDev d = makeDrawDev(ctx, plan);
     // Stage the zeroed counters and the descriptors through pinned memory;
-    // a kernel parameter carries them to the device (a copy when the block is
-    // above 8 KB, and in a graph capture, whose copy node reads the stage at
-    // every replay).
+    // for a blocking draw a kernel parameter carries them to the device, else
+    // (and for blocks above 8 KB) a copy; in a graph capture the copy node
+    // reads the stage at every replay.
     size_t n1 = plan.inst.size() + 1;
     size_t instBytes = sizeof(InstanceDev) * plan.inst.size();
     const size_t cb = counterBytes(plan);
@@ -780,9 +784,10 @@ cr_status launchDrawWith(cr_context* ctx, const Plan& plan, cudaStream_t stream,
     memcpy(hp + 12 * n1, plan.binPrefix.data(), 4 * n1);
     memcpy(hp + 16 * n1, plan.tilePrefix.data(), 4 * n1);
     const size_t blockBytes = cb + instBytes + kPrefixBytesPerInstance * n1;
-    if (blockBytes <= 1024 && !capturing(stream))
+    writeKernel = writeKernel && !capturing(stream);
+    if (writeKernel && blockBytes <= 1024)
         CR_CUDA(writeBlock<256>(stage, ctx->drawBlock.ptr, blockBytes, stream), "block write");
-    else if (blockBytes <= 8192 && !capturing(stream))
+    else if (writeKernel && blockBytes <= 8192)
         CR_CUDA(writeBlock<2048>(stage, ctx->drawBlock.ptr, blockBytes, stream), "block write");
     else
         CR_CUDA(cudaMemcpyAsync(ctx->drawBlock.ptr, stage, blockBytes, cudaMemcpyHostToDevice, stream),
@@ -820,11 +825,11 @@ cr_status launchDrawWith(cr_context* ctx, const Plan& plan, cudaStream_t stream,
     return CR_OK;
 }
 
-cr_status launchDraw(cr_context* ctx, const Plan& plan, cudaStream_t stream) {
+cr_status launchDraw(cr_context* ctx, const Plan& plan, cudaStream_t stream, bool sync) {
     const int slot = ctx->stageNext;
     ctx->stageNext = (slot + 1) % cr_context::kStageSlots;
     if (ctx->stageUsed[slot]) CR_CUDA(cudaEventSynchronize(ctx->stageDone[slot]), "cudaEventSynchronize");
-    cr_status st = launchDrawWith(ctx, plan, stream, ctx->hostStage[slot], ctx->hostCounters, ctx->stageTiming);
+    cr_status st = launchDrawWith(ctx, plan, stream, ctx->hostStage[slot], ctx->hostCounters, ctx->stageTiming, sync);
     if (st != CR_OK) return st;
     ctx->drawn = true;
     CR_CUDA(cudaEventRecord(ctx->stageDone[slot], stream), "cudaEventRecord");
@@ -858,7 +863,7 @@ cr_status drawPlan(cr_context* ctx, const Plan& plan, cudaStream_t stream, bool 
     ctx->last.num_bins = plan.totalBins;
     ctx->last.num_tiles = plan.totalTiles;
     for (int reruns = 0;; reruns++) {
-        st = launchDraw(ctx, plan, stream);
+        st = launchDraw(ctx, plan, stream, sync);
         if (st != CR_OK) return st;
         if (!sync) {
             ctx->last.reruns = 0;
@@ -1013,7 +1018,7 @@ cr_status cr_batch_graph_create(cr_context* ctx, const cr_instance* instances, i
     cudaStreamSynchronize((cudaStream_t)stream);
     e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        st = launchDrawWith(ctx, g->plan, cap, g->stage, g->counters, false);
+        st = launchDrawWith(ctx, g->plan, cap, g->stage, g->counters, false, false);
         cudaError_t e2 = cudaStreamEndCapture(cap, &g->graph);
         if (st == CR_OK && e2 != cudaSuccess) st = cudaFail(ctx, e2, "cudaStreamEndCapture");
     } else {
