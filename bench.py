@@ -44,6 +44,9 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 PKG = "cudaraster-linux_gb300"
 
+# The library's kernels in one blocking draw of the soup: the draw-block write,
+# setup, bin count / scan / scatter, coarse count / scan / scatter and fine.
+KERNELS_PER_DRAW = 9
 METRIC = "frames/s & Mtri/s on 1 GB300: batched+predicted vs plain, bit-exact framebuffers"
 WORKLOAD = {"workload": "plain path at scale: 1M-triangle random soup, 1920x1080, 1 spp, Gouraud, depth LESS, opaque",
             "num_tris": 1_000_000, "width": 1920, "height": 1080, "samples": 1, "pipe": "PixelPipe_gouraud",
@@ -474,7 +477,7 @@ def main():
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_total / args.steps, 4)},
             "roofline": roofline, "clocks": clk.summary(),
             "ms_per_step_with_stage_events": round(staged_ms / stage_steps, 4),
-            "gpu_launches": 8 * args.steps, "counters": counters, "tuning": tuning}
+            "gpu_launches": KERNELS_PER_DRAW * args.steps, "counters": counters, "tuning": tuning}
     if not args.no_batch:
         scenes = importlib.import_module(PKG + ".scenes")
         batch = workloads.Batch(scenes.batch(64, seed=4))
