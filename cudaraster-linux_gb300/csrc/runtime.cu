@@ -806,20 +806,21 @@ cr_status launchDrawWith(cr_context* ctx, const Plan& plan, cudaStream_t stream,
         cudaGetLastError();
         devHostCounters = nullptr;
     }
+    bool written = false;
     int warps = ctx->tuning.fine_warps > 0 ? ctx->tuning.fine_warps : 8;
     for (size_t gi = 0; gi < plan.groups.size(); gi++) {
         const Plan::Group& g = plan.groups[gi];
         int ctas = ctx->tuning.fine_ctas_per_sm > 0 ? ctx->tuning.fine_ctas_per_sm : g.pipe->fineOccupancy(warps);
         DrawDev dg = d;
-        if (devHostCounters && g.tileEnd > g.tileBegin) {
+        if (!written && devHostCounters && g.tileEnd > g.tileBegin) {
             dg.hostCounters = devHostCounters;
-            devHostCounters = nullptr;
+            written = true;
         }
         CR_CUDA(g.pipe->launchFine(dg, (int)gi, g.tileBegin, g.tileEnd, warps, ctas, ctx->numSMs, stream), "fine launch");
     }
     if (events) CR_CUDA(cudaEventRecord(ctx->ev[4], stream), "cudaEventRecord");
     ctx->eventsRecorded = events;
-    if (devHostCounters)
+    if (!written)
         CR_CUDA(cudaMemcpyAsync(hostCounters, ctx->drawBlock.ptr, sizeof(Counters), cudaMemcpyDeviceToHost, stream),
                 "cudaMemcpyAsync");
     return CR_OK;
