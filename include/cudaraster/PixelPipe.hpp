@@ -192,8 +192,11 @@ public:
 // shader that never discards, the colour and depth of every sample depend
 // only on the front-most covering fragment (earliest in submission order on
 // ties), so the fine stage resolves visibility first and shades each sample's
-// winner once. The defaults are the safe ones; specialise them for your own
-// shaders when the facts hold.
+// winner once. A fragment shader that never discards also lets the ordered
+// path (blending pipes) drop, at one sample per pixel, the fragments that
+// would fail the depth test behind an earlier one of the same batch. The
+// defaults are the safe ones; specialise them for your own shaders only when
+// the facts hold (a shader that can discard must keep mayDiscard true).
 template <class BS> struct BlendShaderTraits { static constexpr bool needsDst = true; };
 template <> struct BlendShaderTraits<BlendReplace> { static constexpr bool needsDst = false; };
 template <> struct BlendShaderTraits<BlendDepthOnly> { static constexpr bool needsDst = false; };
